@@ -1,0 +1,229 @@
+"""ctypes bindings for the CPU oracle (test infrastructure only).
+
+``Oracle()`` loads oracle/_build/libhbt_oracle.so, the C restatement of the
+reference unbinding path (hbt_oracle.c).  ``Oracle(reference=True)`` loads
+oracle/_ref/libhbt_ref.so, the reference's own Subhalo_t::Unbind compiled
+from its unmodified sources (only present where the reference is).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU legs import this
+module; the product package never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libhbt_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libhbt_ref.so")
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("softening", C.c_double),
+        ("open_angle", C.c_double),
+        ("bound_mass_precision", C.c_double),
+        ("min_num_part", C.c_int64),
+        ("max_sample_size", C.c_int64),
+        ("refine_mostbound", C.c_int32),
+        ("periodic", C.c_int32),
+        ("box_size", C.c_double),
+        ("G", C.c_double),
+        ("hubble", C.c_double),
+        ("scale_factor", C.c_double),
+    ]
+
+
+class State(C.Structure):
+    _fields_ = [
+        ("ref_pos", C.c_float * 3),
+        ("ref_vel", C.c_float * 3),
+        ("mostbound_pos", C.c_float * 3),
+        ("mostbound_vel", C.c_float * 3),
+        ("mostbound_id", C.c_int64),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("nbound", C.c_int64),
+        ("mbound", C.c_float),
+        ("ref_pos", C.c_float * 3),
+        ("ref_vel", C.c_float * 3),
+        ("mostbound_pos", C.c_float * 3),
+        ("mostbound_vel", C.c_float * 3),
+        ("specific_potential", C.c_float),
+        ("specific_kinetic", C.c_float),
+        ("specific_angmom", C.c_float * 3),
+        ("nbound_type", C.c_int64 * 6),
+        ("mbound_type", C.c_float * 6),
+        ("iterations", C.c_int32),
+        ("disrupted", C.c_int32),
+        ("converged", C.c_int32),
+        ("too_few", C.c_int32),
+        ("evaluations", C.c_int64),
+        ("interactions", C.c_int64),
+    ]
+
+
+def result_dict(r: Result) -> dict:
+    out = {}
+    for name, _ in Result._fields_:
+        v = getattr(r, name)
+        out[name] = np.array(list(v)) if hasattr(v, "__len__") else v
+    return out
+
+
+def make_params(p: dict) -> Params:
+    return Params(
+        softening=p["softening"], open_angle=p["open_angle"],
+        bound_mass_precision=p["bound_mass_precision"],
+        min_num_part=int(p["min_num_part"]), max_sample_size=int(p["max_sample_size"]),
+        refine_mostbound=int(p["refine_mostbound"]), periodic=int(p["periodic"]),
+        box_size=p["box_size"], G=p["G"], hubble=p["hubble"],
+        scale_factor=p["scale_factor"])
+
+
+def make_state(ref_pos, ref_vel, mb_pos, mb_vel, mb_id) -> State:
+    s = State()
+    for k in range(3):
+        s.ref_pos[k] = ref_pos[k]
+        s.ref_vel[k] = ref_vel[k]
+        s.mostbound_pos[k] = mb_pos[k]
+        s.mostbound_vel[k] = mb_vel[k]
+    s.mostbound_id = int(mb_id)
+    return s
+
+
+def build(reference: bool = False) -> None:
+    """Compile the oracle (and, with reference=True, the reference harness)."""
+    target = ["ref"] if reference else []
+    subprocess.run(["make", "-s", "-C", HERE, "-j8"] + target, check=True)
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Oracle:
+    """The C restatement (default) or the reference build (reference=True)."""
+
+    def __init__(self, reference: bool = False):
+        so = REF_SO if reference else ORACLE_SO
+        if not os.path.exists(so):
+            build(reference)
+        self.reference = reference
+        self.lib = C.CDLL(so)
+        pre = "ref_" if reference else "hbto_"
+        self._unbind = getattr(self.lib, pre + "unbind")
+        self._batch = getattr(self.lib, pre + "unbind_batch")
+        self._energies = getattr(self.lib, pre + "binding_energies")
+        self._srand48 = getattr(self.lib, pre + "srand48")
+        self._shuffle = self.lib.hbto_reference_shuffle
+        self._shuffle.argtypes = [C.c_int64, C.c_uint, C.POINTER(C.c_int64)]
+        if not reference:
+            self._partition = self.lib.hbto_partition
+            self._partition.restype = C.c_int64
+
+    # -- helpers ----------------------------------------------------------
+    def srand48(self, seed: int) -> None:
+        self._srand48(C.c_long(seed))
+
+    def reference_shuffle(self, n: int, seed: int) -> np.ndarray:
+        perm = np.empty(max(n, 1), np.int64)
+        self._shuffle(n, seed, _p(perm, C.c_int64))
+        return perm[:n]
+
+    def partition(self, E: np.ndarray):
+        E = np.ascontiguousarray(E, np.float32).copy()
+        idx = np.arange(len(E), dtype=np.int64)
+        nb = self._partition(_p(E, C.c_float), _p(idx, C.c_int64), C.c_int64(len(E)))
+        return int(nb), E, idx
+
+    # -- the path -----------------------------------------------------------
+    def unbind(self, params: dict, sub: dict, nthreads: int = 1, shuffle_seed: int = 0,
+               drand_seed: int = 1):
+        """Unbind one subhalo.  ``sub`` holds id, pos (n,3), vel (n,3), mass,
+        type, ref_pos, ref_vel, mostbound_pos, mostbound_vel (and optionally
+        mostbound_id).  For the C restatement the particles are taken as given
+        (already shuffled when sampling applies); the reference harness takes
+        them before the shuffle and shuffles with ``shuffle_seed``."""
+        n = len(sub["mass"])
+        ids = np.ascontiguousarray(sub["id"], np.int64)
+        pos = np.ascontiguousarray(sub["pos"], np.float32).reshape(-1)
+        vel = np.ascontiguousarray(sub["vel"], np.float32).reshape(-1)
+        mass = np.ascontiguousarray(sub["mass"], np.float32)
+        typ = np.ascontiguousarray(sub.get("type", np.ones(n, np.int32)), np.int32)
+        mb_id = sub.get("mostbound_id", ids[0] if n else -1)
+        st = make_state(sub["ref_pos"], sub["ref_vel"], sub["mostbound_pos"],
+                        sub["mostbound_vel"], mb_id)
+        order = np.zeros(max(n, 1), np.int64)
+        energy = np.zeros(max(n, 1), np.float32)
+        res = Result()
+        par = make_params(params)
+        self.srand48(drand_seed)
+        args = [C.byref(par), C.c_int64(n), _p(ids, C.c_int64), _p(pos, C.c_float),
+                _p(vel, C.c_float), _p(mass, C.c_float), _p(typ, C.c_int32), C.byref(st),
+                _p(order, C.c_int64), _p(energy, C.c_float), C.byref(res), C.c_int(nthreads)]
+        if self.reference:
+            args.append(C.c_uint(shuffle_seed))
+        rc = self._unbind(*args)
+        if rc != 0:
+            raise RuntimeError(f"oracle unbind failed with status {rc}")
+        return order[:n], energy[:n], result_dict(res)
+
+    def unbind_batch(self, params: dict, batch: dict, nthreads: int = 0,
+                     shuffle_seed: int = 0, drand_seed: int = 1):
+        """Unbind every subhalo of a batch (see hbtplus_gb300.synthetic)."""
+        off = np.ascontiguousarray(batch["offsets"], np.int64)
+        nsub = len(off) - 1
+        ntot = int(off[-1])
+        ids = np.ascontiguousarray(batch["id"], np.int64)
+        pos = np.ascontiguousarray(batch["pos"], np.float32).reshape(-1)
+        vel = np.ascontiguousarray(batch["vel"], np.float32).reshape(-1)
+        mass = np.ascontiguousarray(batch["mass"], np.float32)
+        typ = np.ascontiguousarray(batch.get("type", np.ones(ntot, np.int32)), np.int32)
+        sts = (State * max(nsub, 1))()
+        for s in range(nsub):
+            o = int(off[s])
+            mb_id = batch["mostbound_id"][s] if "mostbound_id" in batch else (
+                ids[o] if off[s + 1] > o else -1)
+            sts[s] = make_state(batch["ref_pos"][s], batch["ref_vel"][s],
+                                batch["mostbound_pos"][s], batch["mostbound_vel"][s], mb_id)
+        order = np.zeros(max(ntot, 1), np.int64)
+        energy = np.zeros(max(ntot, 1), np.float32)
+        res = (Result * max(nsub, 1))()
+        par = make_params(params)
+        self.srand48(drand_seed)
+        args = [C.byref(par), C.c_int64(nsub), _p(off, C.c_int64), _p(ids, C.c_int64),
+                _p(pos, C.c_float), _p(vel, C.c_float), _p(mass, C.c_float),
+                _p(typ, C.c_int32), sts, _p(order, C.c_int64), _p(energy, C.c_float), res,
+                C.c_int(nthreads)]
+        if self.reference:
+            args.append(C.c_uint(shuffle_seed))
+        rc = self._batch(*args)
+        if rc != 0:
+            raise RuntimeError(f"oracle batch unbind failed with status {rc}")
+        return order[:ntot], energy[:ntot], [result_dict(res[s]) for s in range(nsub)]
+
+    def binding_energies(self, params: dict, pos, vel, mass, ref_pos, ref_vel,
+                         nthreads: int = 1, drand_seed: int = 1):
+        """First-pass energies and potentials of every particle (tree over all)."""
+        n = len(mass)
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1)
+        vel = np.ascontiguousarray(vel, np.float32).reshape(-1)
+        mass = np.ascontiguousarray(mass, np.float32)
+        rp = np.ascontiguousarray(ref_pos, np.float32)
+        rv = np.ascontiguousarray(ref_vel, np.float32)
+        E = np.zeros(max(n, 1), np.float32)
+        pot = np.zeros(max(n, 1), np.float64)
+        cnt = C.c_int64(0)
+        par = make_params(params)
+        self.srand48(drand_seed)
+        self._energies(C.byref(par), C.c_int64(n), _p(pos, C.c_float), _p(vel, C.c_float),
+                       _p(mass, C.c_float), _p(rp, C.c_float), _p(rv, C.c_float),
+                       _p(E, C.c_float), _p(pot, C.c_double), C.byref(cnt), C.c_int(nthreads))
+        return E[:n], pot[:n], cnt.value

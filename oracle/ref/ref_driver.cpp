@@ -1,0 +1,251 @@
+/* ref_driver.cpp -- harness around the reference's own Subhalo_t::Unbind.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Compiled (by oracle/Makefile, target `ref`)
+ * together with the unmodified reference sources where they lie, into
+ * oracle/_ref/libhbt_ref.so, which is never committed.  It exports the
+ * entry points of oracle/hbt_oracle.h with the prefix ref_, so that the C
+ * restatement can be pinned against the reference on identical inputs and
+ * the reference can be timed as the CPU baseline.
+ *
+ * Differences from the hbto_ entry points:
+ *   - ref_unbind/ref_unbind_batch take the particles in their order BEFORE
+ *     the sampling shuffle (position 0 = previous most-bound) plus the seed
+ *     for srand(); the reference shuffles them itself
+ *     (src/subhalo_unbind.cpp:302).
+ *   - iterations/evaluations/interactions are not available (left 0).
+ */
+#include <omp.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "config_parser.h"
+#include "datatypes.h"
+#include "gravity_tree.h"
+#include "snapshot.h"
+#include "subhalo.h"
+
+#include "../hbt_oracle.h"
+
+namespace {
+
+/* The reference's configuration as ParseConfigFile leaves it
+ * (src/config_parser.cpp:95-103), for the unbinding subset. */
+void setup(const hbto_params *p)
+{
+  HBTConfig.SofteningHalo = p->softening;
+  HBTConfig.TreeNodeOpenAngle = p->open_angle;
+  HBTConfig.BoundMassPrecision = p->bound_mass_precision;
+  HBTConfig.MinNumPartOfSub = (int)p->min_num_part;
+  HBTConfig.MaxSampleSizeOfPotentialEstimate = p->max_sample_size;
+  HBTConfig.RefineMostboundParticle = p->refine_mostbound != 0;
+  HBTConfig.PeriodicBoundaryOn = p->periodic != 0;
+  HBTConfig.BoxSize = p->box_size;
+  PhysicalConst::G = p->G;
+  HBTConfig.BoxHalf = HBTConfig.BoxSize / 2.;
+  HBTConfig.TreeNodeResolution = HBTConfig.SofteningHalo * 0.1;
+  HBTConfig.TreeNodeResolutionHalf = HBTConfig.TreeNodeResolution / 2.;
+  HBTConfig.TreeNodeOpenAngleSquare = HBTConfig.TreeNodeOpenAngle * HBTConfig.TreeNodeOpenAngle;
+}
+
+/* The snapshot handed to Unbind: only Cosmology and the snapshot index are read. */
+class Epoch_t : public Snapshot_t
+{
+public:
+  Epoch_t(const hbto_params *p)
+  {
+    Cosmology.ScaleFactor = p->scale_factor;
+    Cosmology.Hz = p->hubble;
+    Cosmology.OmegaM0 = 0.3;
+    Cosmology.OmegaLambda0 = 0.7;
+    Cosmology.OmegaZ = 0.3;
+    SnapshotIndex = 1;
+    SnapshotId = 1;
+  }
+  HBTInt size() const { return 0; }
+  const HBTxyz &GetComovingPosition(const HBTInt) const { return dummy; }
+  const HBTxyz &GetPhysicalVelocity(const HBTInt) const { return dummy; }
+  HBTReal GetMass(const HBTInt) const { return 0; }
+
+private:
+  HBTxyz dummy{{0, 0, 0}};
+};
+
+/* A plain particle array viewed as a Snapshot_t, for the tree-only entry. */
+class ArraySnapshot_t : public Snapshot_t
+{
+public:
+  ArraySnapshot_t(const hbto_params *p, int64_t n, const float *pos, const float *vel,
+                  const float *mass)
+      : P(n), V(n), M(mass, mass + n)
+  {
+    Cosmology.ScaleFactor = p->scale_factor;
+    Cosmology.Hz = p->hubble;
+    for (int64_t i = 0; i < n; i++)
+      for (int j = 0; j < 3; j++) {
+        P[i][j] = pos[3 * i + j];
+        V[i][j] = vel[3 * i + j];
+      }
+  }
+  HBTInt size() const { return P.size(); }
+  const HBTxyz &GetComovingPosition(const HBTInt i) const { return P[i]; }
+  const HBTxyz &GetPhysicalVelocity(const HBTInt i) const { return V[i]; }
+  HBTReal GetMass(const HBTInt i) const { return M[i]; }
+  std::vector<HBTxyz> P, V;
+  std::vector<HBTReal> M;
+};
+
+void fill_subhalo(Subhalo_t &sub, int64_t n, const int64_t *id, const float *pos, const float *vel,
+                  const float *mass, const int32_t *type, const hbto_state *st)
+{
+  sub.Particles.resize(n);
+  for (int64_t i = 0; i < n; i++) {
+    Particle_t &p = sub.Particles[i];
+    p.Id = id[i];
+    for (int j = 0; j < 3; j++) {
+      p.ComovingPosition[j] = pos[3 * i + j];
+      p.PhysicalVelocity[j] = vel[3 * i + j];
+    }
+    p.Mass = mass[i];
+    p.Type = (ParticleType_t)(type ? type[i] : 1);
+  }
+  sub.Nbound = n;
+  for (int j = 0; j < 3; j++) {
+    sub.ComovingAveragePosition[j] = st->ref_pos[j];
+    sub.PhysicalAverageVelocity[j] = st->ref_vel[j];
+    sub.ComovingMostBoundPosition[j] = st->mostbound_pos[j];
+    sub.PhysicalMostBoundVelocity[j] = st->mostbound_vel[j];
+  }
+}
+
+/* Output ids are mapped back to input positions through the caller's id list
+ * (ids are unique in every input the tests use). */
+void read_subhalo(const Subhalo_t &sub, int64_t n, const int64_t *id_sorted_pos,
+                  const int64_t *id_sorted, int64_t *order, float *energy, hbto_result *res,
+                  int64_t nin)
+{
+  std::memset(res, 0, sizeof(*res));
+  res->nbound = sub.Nbound;
+  res->mbound = sub.Mbound;
+  for (int j = 0; j < 3; j++) {
+    res->ref_pos[j] = sub.ComovingAveragePosition[j];
+    res->ref_vel[j] = sub.PhysicalAverageVelocity[j];
+    res->mostbound_pos[j] = sub.ComovingMostBoundPosition[j];
+    res->mostbound_vel[j] = sub.PhysicalMostBoundVelocity[j];
+    res->specific_angmom[j] = sub.SpecificAngularMomentum[j];
+  }
+  res->specific_potential = sub.SpecificSelfPotentialEnergy;
+  res->specific_kinetic = sub.SpecificSelfKineticEnergy;
+  for (int k = 0; k < 6; k++) {
+    res->nbound_type[k] = sub.NboundType[k];
+    res->mbound_type[k] = sub.MboundType[k];
+  }
+  for (int64_t i = 0; i < n; i++) {
+    int64_t key = sub.Particles[i].Id;
+    const int64_t *it = std::lower_bound(id_sorted, id_sorted + nin, key);
+    order[i] = (it != id_sorted + nin && *it == key) ? id_sorted_pos[it - id_sorted] : -1;
+    energy[i] = i < (int64_t)sub.Energies.size() ? sub.Energies[i] : NAN;
+  }
+}
+
+void sorted_ids(int64_t n, const int64_t *id, std::vector<int64_t> &ids, std::vector<int64_t> &pos)
+{
+  std::vector<std::pair<int64_t, int64_t>> v(n);
+  for (int64_t i = 0; i < n; i++) v[i] = std::make_pair(id[i], i);
+  std::sort(v.begin(), v.end());
+  ids.resize(n);
+  pos.resize(n);
+  for (int64_t i = 0; i < n; i++) {
+    ids[i] = v[i].first;
+    pos[i] = v[i].second;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int ref_unbind(const hbto_params *par, int64_t n, const int64_t *id, const float *pos,
+               const float *vel, const float *mass, const int32_t *type, const hbto_state *st,
+               int64_t *order, float *energy, hbto_result *res, int nthreads,
+               unsigned shuffle_seed)
+{
+  setup(par);
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  omp_set_max_active_levels(1);
+  Epoch_t epoch(par);
+  Subhalo_t sub;
+  fill_subhalo(sub, n, id, pos, vel, mass, type, st);
+  srand(shuffle_seed);
+  sub.Unbind(epoch);
+  std::vector<int64_t> ids, ipos;
+  sorted_ids(n, id, ids, ipos);
+  read_subhalo(sub, n, ipos.data(), ids.data(), order, energy, res, n);
+  res->too_few = n < par->min_num_part;
+  res->disrupted = (n >= 2 && sub.Nbound == 1);
+  res->converged = (n >= 2 && !res->disrupted);
+  return 0;
+}
+
+int ref_unbind_batch(const hbto_params *par, int64_t nsub, const int64_t *off, const int64_t *id,
+                     const float *pos, const float *vel, const float *mass, const int32_t *type,
+                     const hbto_state *st, int64_t *order, float *energy, hbto_result *res,
+                     int nthreads, unsigned shuffle_seed)
+{
+  setup(par);
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  omp_set_max_active_levels(1);
+  Epoch_t epoch(par);
+  std::vector<Subhalo_t> subs(nsub);
+  for (int64_t s = 0; s < nsub; s++) {
+    const int64_t o = off[s];
+    fill_subhalo(subs[s], off[s + 1] - o, id + o, pos + 3 * o, vel + 3 * o, mass + o,
+                 type ? type + o : nullptr, st + s);
+  }
+  srand(shuffle_seed);
+  /* the field-subhalo loop of SubhaloSnapshot_t::RefineParticles
+   * (src/subhalo_unbind.cpp:495-503) */
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t s = 0; s < nsub; s++) subs[s].Unbind(epoch);
+  for (int64_t s = 0; s < nsub; s++) {
+    const int64_t o = off[s], m = off[s + 1] - off[s];
+    std::vector<int64_t> ids, ipos;
+    sorted_ids(m, id + o, ids, ipos);
+    read_subhalo(subs[s], m, ipos.data(), ids.data(), order + o, energy + o, res + s, m);
+    res[s].too_few = m < par->min_num_part;
+    res[s].disrupted = (m >= 2 && subs[s].Nbound == 1);
+    res[s].converged = (m >= 2 && !res[s].disrupted);
+  }
+  return 0;
+}
+
+int ref_binding_energies(const hbto_params *par, int64_t n, const float *pos, const float *vel,
+                         const float *mass, const float ref_pos[3], const float ref_vel[3],
+                         float *energy, double *potential, int64_t *interactions, int nthreads)
+{
+  setup(par);
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  ArraySnapshot_t snap(par, n, pos, vel, mass);
+  GravityTree_t tree;
+  tree.Reserve(n);
+  tree.Build(snap);
+  HBTxyz rp, rv;
+  for (int j = 0; j < 3; j++) {
+    rp[j] = ref_pos[j];
+    rv[j] = ref_vel[j];
+  }
+#pragma omp parallel for if (n > 100)
+  for (int64_t i = 0; i < n; i++) {
+    if (potential) potential[i] = tree.EvaluatePotential(snap.P[i], snap.M[i]);
+    energy[i] = tree.BindingEnergy(snap.P[i], snap.V[i], rp, rv, snap.M[i]);
+  }
+  if (interactions) *interactions = 0;
+  return 0;
+}
+
+void ref_srand48(long seed) { srand48(seed); }
+
+}  // extern "C"
