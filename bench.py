@@ -1,0 +1,426 @@
+"""Benchmark of the batched subhalo-unbinding path on GB300.
+
+Workload (one step): unbinding of the 2000-subhalo batch -- sizes drawn from
+dN/dlnN ~ N^-0.9 on [20, 2e5], NFW haloes with Jeans velocities and 20%
+unbound contaminants, centres uniform in a 100 Mpc/h periodic box (about 5%
+straddling a face) -- in one hbtu_unbind_batch call (seeded synthetic data:
+no public particle suite exists for this path).  Parameters are the
+reference's defaults with the exact tree (MaxSampleSizeOfPotentialEstimate 0),
+softening 0.002 Mpc/h, opening angle 0.45.
+
+  value  subhalo unbinds/s with inputs resident in HBM, CUDA events on the
+         library's stream, L2 flushed (256 MB write) before every timed step
+  e2e    the same through the C ABI with pinned host buffers: host->device
+         copy of the particles and device->host read of order, energies and
+         per-subhalo results inside the timed region
+  plain  the same batch unbound one subhalo per call (hbtu_unbind)
+  cpu_baseline  the reference CPU path on the same batch on this host's cores
+
+python bench.py [--steps K] [--warmup W] [--impl reference]; under torchrun
+every rank unbinds its own batch (independent subhaloes: weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("subhalo unbinds/s & particle-potentials/s, batched vs plain, same GB300, "
+          "≤1e-4 mass err")
+UNIT = "subhalo unbinds/s"
+FLOPS_PER_INTERACTION = 14  # 3 sub, 5 for r^2, 4 for rsqrt, 2 for the potential update
+HBM_BYTES_PER_EVALUATION = 44  # read pos, vel, mass (28 B); write E and index (16 B)
+FP32_LANES_PER_SM = 128
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nsub", type=int, default=2000)
+    ap.add_argument("--workload", default="batch", choices=["batch", "single"],
+                    help="batch: the 2000-subhalo batch (default); single: the isolated "
+                         "1e5-particle NFW subhalo (+10%% contaminants)")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(nsub: int, rank: int, kind: str = "batch"):
+    from hbtplus_gb300 import synthetic as S
+    if kind == "single":
+        return S.concat([S.single_subhalo(seed=20261203 + 1000 * rank)]), S.default_params()
+    b = S.subhalo_batch(nsub=nsub, seed=20261204 + 1000 * rank)
+    return b, S.default_params()
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_reference_time(params, batch, threads):
+    """(seconds, kind) of one unbinding of the batch by the reference CPU path:
+    the reference's own Unbind when its harness is built here, else the C
+    restatement (oracle/hbt_oracle.c), halo-parallel on `threads` threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    kind = "reference" if os.path.exists(O.REF_SO) else "port"
+    if kind == "port" and not os.path.exists(O.ORACLE_SO):
+        O.build(reference=False)
+    orc = O.Oracle(reference=(kind == "reference"))
+    t = time.perf_counter()
+    _, _, res = orc.unbind_batch(params, batch, nthreads=threads)
+    return time.perf_counter() - t, kind, res
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def run_reference_arm(args, ws, rank):
+    if rank != 0:
+        return
+    batch, params = workload(args.nsub, 0, args.workload)
+    threads = cpu_threads()
+    for _ in range(args.warmup):
+        cpu_reference_time(params, batch, threads)
+    times, kind = [], "port"
+    for _ in range(args.steps):
+        t, kind, _ = cpu_reference_time(params, batch, threads)
+        times.append(t)
+    total = sum(times)
+    nsub = len(batch["offsets"]) - 1
+    value = nsub * args.steps / total
+    nsum = int(batch["offsets"][-1])
+    sample = (f"the full {nsub}-subhalo workload ({nsum} particles) per step, "
+              f"halo-parallel OpenMP schedule(dynamic,1)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config_of(args, batch),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args, batch):
+    nsub = len(batch["offsets"]) - 1
+    if args.workload == "single":
+        name = ("single subhalo: 1e5-particle NFW (r200 0.2 Mpc/h, c 10) + 10% contaminants, "
+                "100 Mpc/h periodic box")
+    else:
+        name = (f"{nsub}-subhalo batch: dN/dlnN ~ N^-0.9 on [20, 2e5], NFW + Jeans, "
+                "20% contaminants, 100 Mpc/h periodic box")
+    return {"workload": name,
+            "nsub": nsub, "particles": int(batch["offsets"][-1]),
+            "max_subhalo": int(np.max(np.diff(batch["offsets"]))),
+            "softening": 0.002, "open_angle": 0.45, "max_sample_size": 0,
+            "precision": args.precision, "l2": "flushed before each timed step (256 MB write)"}
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    if args.impl == "reference":
+        run_reference_arm(args, ws, rank)
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    import torch
+
+    from hbtplus_gb300 import _lib
+    from hbtplus_gb300 import unbind as U
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    batch, params = workload(args.nsub, rank, args.workload)
+    nsub = len(batch["offsets"]) - 1
+    ntot = int(batch["offsets"][-1])
+    prec = 1 if args.precision == "fp64" else 0
+    ub = U.Unbinder(params, precision=prec, device=local)
+    stream = torch.cuda.current_stream(dev)
+    ub.set_stream(stream.cuda_stream)
+
+    # -- device-resident inputs and outputs ---------------------------------
+    d_in = {k: torch.from_numpy(np.ascontiguousarray(batch[k])).to(dev)
+            for k in ("id", "pos", "vel", "mass", "type")}
+    d_out = dict(order=torch.empty(ntot, dtype=torch.int64, device=dev),
+                 energy=torch.empty(ntot, dtype=torch.float32, device=dev),
+                 res=torch.empty(nsub * C.sizeof(_lib.hbtu_result), dtype=torch.uint8,
+                                 device=dev))
+    states = ub.make_states(batch)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    def step():
+        ub.unbind_batch_device(d_in, batch["offsets"], states, d_out)
+
+    # reference interactions/evaluations of this batch (identical walk): host call
+    _, _, host_res = ub.unbind_batch(batch)
+    interactions = sum(int(r["interactions"]) for r in host_res)
+    evaluations = sum(int(r["evaluations"]) for r in host_res)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ub.set_timing(True)
+    ub.reset_stats()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            times.append((e0, e1))
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in times]
+    total_ms = sum(step_ms)
+    st = ub.stats()
+    ub.set_timing(False)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    ms_per_step = total_ms / args.steps
+    value = ws * nsub / (ms_per_step / 1e3)
+    clocks = clk.summary()
+
+    # -- roofline of the dominant kernel (the energy walk) ----------------------
+    walk_ms = st["walk_ms"] / args.steps
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = clocks.get("sm_mhz") or 1965.0
+    fp32_peak = sm_count * FP32_LANES_PER_SM * 2 * mhz * 1e6 / 1e12
+    achieved = interactions * FLOPS_PER_INTERACTION / (walk_ms / 1e3) / 1e12 if walk_ms else 0.0
+    peaks, peak_kind = measured_peaks()
+    hbm_achieved = evaluations * HBM_BYTES_PER_EVALUATION / (walk_ms / 1e3) / 1e9 if walk_ms else 0
+    roofline = {
+        "kernel": "k_walk (Barnes-Hut energy walk)",
+        "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+        "frac": achieved / fp32_peak if fp32_peak else None,
+        "peak_source": f"{sm_count} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 flop at the "
+                       f"measured median SM clock {mhz:.0f} MHz (FP32 FMA rate; no FP32 figure "
+                       "in MEASURED_PEAKS.json)",
+        "traffic": None,
+        "flops_per_interaction": FLOPS_PER_INTERACTION,
+        "interactions_per_step": interactions, "walk_ms_per_step": walk_ms,
+        "walk_share_of_step": walk_ms / ms_per_step if ms_per_step else None,
+        "hbm": {"bound": "hbm", "achieved": hbm_achieved, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": hbm_achieved / peaks["hbm_gbs"],
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                "bytes_per_evaluation": HBM_BYTES_PER_EVALUATION},
+    }
+
+    # -- e2e: host buffers through the C ABI, pinned memory -----------------------
+    pin = {k: torch.from_numpy(np.ascontiguousarray(batch[k])).pin_memory()
+           for k in ("id", "pos", "vel", "mass", "type")}
+    out_order = torch.empty(ntot, dtype=torch.int64).pin_memory()
+    out_energy = torch.empty(ntot, dtype=torch.float32).pin_memory()
+    out_res = (_lib.hbtu_result * nsub)()
+    offsets = np.ascontiguousarray(batch["offsets"], np.int64)
+    p_host = _lib.hbtu_particles(id=pin["id"].data_ptr(), pos=pin["pos"].data_ptr(),
+                                 vel=pin["vel"].data_ptr(), mass=pin["mass"].data_ptr(),
+                                 type=pin["type"].data_ptr(), location=_lib.HBTU_HOST,
+                                 reserved=0)
+
+    def e2e_step():
+        rc = ub.lib.hbtu_unbind_batch(ub.handle, C.byref(p_host), nsub, offsets.ctypes.data,
+                                      C.addressof(states), out_order.data_ptr(),
+                                      out_energy.data_ptr(), C.addressof(out_res))
+        _lib.check(rc, ub.handle)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_t) / args.steps
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = sum(int(v.numel() * v.element_size()) for v in pin.values()) + offsets.nbytes + \
+        C.sizeof(states)
+    d2h = ntot * (8 + 4) + nsub * C.sizeof(_lib.hbtu_result)
+    e2e = {"value": ws * nsub / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s}
+
+    # -- plain form: one subhalo per call on the same GB300 ------------------------
+    plain = None
+    if not args.no_plain:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        order_np = np.empty(ntot, np.int64)
+        for s in range(nsub):
+            o0, o1 = int(offsets[s]), int(offsets[s + 1])
+            n = o1 - o0
+            p1 = _lib.hbtu_particles(
+                id=d_in["id"].data_ptr() + 8 * o0, pos=d_in["pos"].data_ptr() + 12 * o0,
+                vel=d_in["vel"].data_ptr() + 12 * o0, mass=d_in["mass"].data_ptr() + 4 * o0,
+                type=d_in["type"].data_ptr() + 4 * o0, location=_lib.HBTU_DEVICE, reserved=0)
+            rc = ub.lib.hbtu_unbind(ub.handle, C.byref(p1), n, C.byref(states[s]),
+                                    d_out["order"].data_ptr() + 8 * o0,
+                                    d_out["energy"].data_ptr() + 4 * o0,
+                                    d_out["res"].data_ptr() + s * C.sizeof(_lib.hbtu_result))
+            _lib.check(rc, ub.handle)
+        torch.cuda.synchronize()
+        plain_s = time.perf_counter() - t0
+        del order_np
+        plain = {"value": nsub / plain_s, "unit": UNIT, "ms_per_step": 1e3 * plain_s,
+                 "form": "hbtu_unbind once per subhalo, device-resident inputs"}
+
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    # -- CPU baseline (reference path on this host's cores) and accuracy ----------------
+    cpu = None
+    accuracy = None
+    if not args.no_cpu:
+        threads = cpu_threads()
+        t_cpu, kind, cres = cpu_reference_time(params, batch, threads)
+        cpu = {"value": nsub / t_cpu, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"the full {nsub}-subhalo workload, one run, halo-parallel "
+                         "OpenMP schedule(dynamic,1) (src/subhalo_unbind.cpp:495-503)",
+               "seconds": t_cpu}
+        rel = [abs(g["mbound"] - c["mbound"]) / c["mbound"] for g, c in zip(host_res, cres)
+               if c["mbound"] > 0]
+        nb_diff = sum(abs(int(g["nbound"]) - int(c["nbound"])) for g, c in zip(host_res, cres))
+        accuracy = {"max_rel_mass_err": max(rel) if rel else 0.0,
+                    "mean_rel_mass_err": float(np.mean(rel)) if rel else 0.0,
+                    "total_nbound_difference": nb_diff,
+                    "iterations_equal": all(g["iterations"] == c["iterations"]
+                                            for g, c in zip(host_res, cres))}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded NFW/Jeans subhaloes, no public suite exists for this path)",
+        "config": config_of(args, batch),
+        "potentials_per_s": ws * evaluations / (ms_per_step / 1e3),
+        "interactions_per_s": ws * interactions / (ms_per_step / 1e3),
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": int(st["kernel_launches"]),
+        "clocks": clocks,
+        "plain": plain,
+        "batched_over_plain": (value / ws) / plain["value"] if plain else None,
+        "accuracy_vs_cpu_reference": accuracy,
+        "phase_ms_per_step": {"tree": st["tree_ms"] / args.steps, "walk": walk_ms,
+                              "loop": st["loop_ms"] / args.steps,
+                              "passes": st["passes"] / args.steps},
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

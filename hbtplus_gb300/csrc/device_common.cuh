@@ -1,0 +1,138 @@
+// device_common.cuh -- device helpers and the per-call context.
+//
+// Arithmetic that decides the bound set follows the reference's float
+// (HBTReal) / double split operation by operation.  nvcc contracts a*b+c into
+// FMA by default, which rounds differently from the reference's separate
+// multiply and add, so every such operation is spelled with an explicit
+// round-to-nearest intrinsic (__fmul_rn, __dadd_rn, ...).
+#pragma once
+#include "hbtu_internal.h"
+
+namespace hbtu {
+
+constexpr int kChunk = 1024;  // elements per reduction chunk
+constexpr int kDone = 0x7fffffff;
+
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// NEAREST (src/config_parser.h:142) on a double / a float operand.
+__device__ __forceinline__ double nearest_d(double x, const DevParams &P)
+{
+  return x > (double)P.boxhalf ? dsub(x, (double)P.box)
+                               : (x < -(double)P.boxhalf ? dadd(x, (double)P.box) : x);
+}
+__device__ __forceinline__ float nearest_f(float x, const DevParams &P)
+{
+  return x > P.boxhalf ? fsub(x, P.box) : (x < -P.boxhalf ? fadd(x, P.box) : x);
+}
+
+// Snapshot_t::RelativeVelocity (src/snapshot.h:100-111), float arithmetic.
+__device__ __forceinline__ void relvel(const float tp[3], const float tv[3], const float rp[3],
+                                       const float rv[3], float dv[3], const DevParams &P)
+{
+  const float ha = fmul(P.Hz, P.a);
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    float dx = fsub(tp[j], rp[j]);
+    if (P.periodic) dx = nearest_f(dx, P);
+    dv[j] = fadd(fsub(tv[j], rv[j]), fmul(ha, dx));
+  }
+}
+
+// VecNorm / VecDot (src/mymath.h:20-21) in float.
+__device__ __forceinline__ float vdot(const float a[3], const float b[3])
+{
+  return fadd(fadd(fmul(a[0], b[0]), fmul(a[1], b[1])), fmul(a[2], b[2]));
+}
+
+// Relative coordinate of an absolute float coordinate: wrapped once in
+// double, then rounded to float.
+__device__ __forceinline__ float rel_coord(float x, float c, const DevParams &P)
+{
+  double d = dsub((double)x, (double)c);
+  if (P.periodic) d = nearest_d(d, P);
+  return __double2float_rn(d);
+}
+
+// Order-preserving 32-bit key of a float (ascending); -0 sorts as +0.
+__device__ __forceinline__ unsigned float_key(float e)
+{
+  unsigned u = __float_as_uint(e == 0.f ? 0.f : e);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ int upper_bound_i(const int *a, int n, int x)
+{
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] <= x)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// The per-call device context: every buffer of the workspace.
+struct Ctx {
+  DevParams P;
+  int N, S;
+  cudaStream_t st;
+  // particles
+  float4 *pm, *vel;
+  long long *id;
+  int *type, *pseg;
+  int *epid, *epid2;
+  float *eE, *eE2, *eR;
+  int *epos_of_pid, *coh_pid;
+  // per segment
+  SegState *seg;
+  PassPlan *plan, *plan_host;
+  int *tree_base, *tgt_base;                 // S+1 each
+  int *tchunk_base, *bchunk_base, *ub_base;  // S+1 each
+  int *seg_off;                              // S+1
+  int *part_info;                            // 8 ints per segment
+  unsigned *chunk_bbox;                      // 6 per chunk
+  double *chunk_sums;                        // 16 per chunk
+  // sort
+  SortBuffers sb;
+  // tree construction
+  int *childL, *childR, *parentI, *parentL, *rfirst, *rlast, *dnode;
+  int *iscell, *cidx, *cskip, *pcell, *pending, *pending0;
+  unsigned long long *mask;
+  long long *X;
+  // nodes (2 per tree particle)
+  float4 *nd_abs, *nd_rel;
+  float *nd_len2;
+  int *nd_skip;
+  // partition
+  long long *pcode, *pX;
+  int *Pk, *Qk;
+  void *scan_tmp;
+  double *pot_out;  // optional: potentials of a full pass (hbtu_binding_energies)
+};
+
+// launchers (tree.cu)
+void launch_bbox_cube(Ctx &c, int max_chunks);
+void launch_tree_build(Ctx &c, const PassPlan &pl);
+// launchers (walk.cu)
+void launch_walk(Ctx &c, const PassPlan &pl);
+// launchers (loop.cu)
+void launch_init(Ctx &c, const float *pos, const float *vel, const float *mass,
+                 const long long *id);
+void launch_plan(Ctx &c, int mode);  // 0 pass, 1 bound chunks, 2 final
+void launch_partition(Ctx &c);
+void launch_averages_control(Ctx &c, int max_passes);
+// which: 0 unbound blocks, 1 bound parts, 2 refined prefixes (keyed by eR)
+void launch_block_sort(Ctx &c, int total, int which);
+void launch_refine_mode(Ctx &c, int enter);
+void launch_finalize(Ctx &c, int64_t *order_out, float *energy_out, hbtu_result *res_dev);
+
+}  // namespace hbtu

@@ -1,0 +1,780 @@
+// loop.cu -- the iterate-until-converged loop of Subhalo_t::Unbind
+// (src/subhalo_unbind.cpp:263-431), for every subhalo of a batch at once.
+//
+// One pass = tree build (tree.cu) + energies (walk.cu) + the kernels here:
+//   partition   PartitionBindingEnergy (:21-58) reproduced exactly: its
+//               two-pointer exchange is a fixed function of the sign pattern
+//               (k-th positive from the left trades with the k-th negative
+//               from the right), computed with prefix counts, no serial scan;
+//   averages    AverageVelocity / AveragePosition (:108-188) as deterministic
+//               FP64 chunk reductions;
+//   control     disruption (:361-379), the sticky correction flag (:383-392),
+//               convergence on the particle count (:395), and the set-up of
+//               the next pass (full :331-356 or correction :312-330);
+//   block sorts the stable energy sorts of the unbound block (:382) and, at
+//               the end, of the bound block (:405);
+//   finalize    the permuted particle order (:409-418), AverageKinematics
+//               (:189-232) and CountParticleTypes (src/subhalo.cpp:400-444).
+#include "device_common.cuh"
+
+namespace hbtu {
+namespace {
+
+constexpr int kLB = 256;
+constexpr int kPlanThreads = 1024;
+constexpr int kSums = 24;  // doubles per reduction chunk
+
+inline unsigned nblk(long long n, int b = kLB) { return (unsigned)((n + b - 1) / b); }
+
+// ---------------------------------------------------------------- helpers
+template <int K>
+__device__ void block_sum(double (&v)[K], double *out)
+{
+  __shared__ double sh[K][kLB / 32];
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int k = 0; k < K; k++) sh[k][w] = v[k];
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double t = 0.;
+    for (int j = 0; j < kLB / 32; j++) t += sh[threadIdx.x][j];
+    out[threadIdx.x] = t;
+  }
+}
+
+// Exclusive scan over segments of up to 4 counters, one block of 1024 threads.
+__device__ void plan_scan4(int S, int (*getter)(const Ctx &, int, int *), const Ctx &c,
+                           int *out0, int *out1, int *out2, int *out3, int *tot)
+{
+  __shared__ int wsum[4][kPlanThreads / 32];
+  const int per = (S + kPlanThreads - 1) / kPlanThreads;
+  const int b = threadIdx.x * per, e = min(S, b + per);
+  int loc[4] = {0, 0, 0, 0}, v[4];
+  for (int s = b; s < e; s++) {
+    getter(c, s, v);
+    for (int k = 0; k < 4; k++) loc[k] += v[k];
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc[4];
+  for (int k = 0; k < 4; k++) {
+    int x = loc[k];
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    inc[k] = x;
+    if (lane == 31) wsum[k][w] = x;
+  }
+  __syncthreads();
+  if (w == 0) {
+    for (int k = 0; k < 4; k++) {
+      int x = wsum[k][lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      wsum[k][lane] = x;
+    }
+  }
+  __syncthreads();
+  int run[4];
+  for (int k = 0; k < 4; k++) run[k] = (w > 0 ? wsum[k][w - 1] : 0) + inc[k] - loc[k];
+  int *outs[4] = {out0, out1, out2, out3};
+  for (int s = b; s < e; s++) {
+    getter(c, s, v);
+    for (int k = 0; k < 4; k++) {
+      if (outs[k]) outs[k][s] = run[k];
+      run[k] += v[k];
+    }
+  }
+  if (threadIdx.x == kPlanThreads - 1) {
+    for (int k = 0; k < 4; k++) {
+      tot[k] = run[k];
+      if (outs[k]) outs[k][S] = run[k];
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- init
+__global__ void k_init(Ctx c, const float *pos, const float *vel, const float *mass,
+                       const long long *id)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.N) return;
+  const int s = upper_bound_i(c.seg_off, c.S + 1, i) - 1;
+  c.pseg[i] = s;
+  c.pm[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], mass[i]);
+  c.vel[i] = make_float4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.f);
+  c.epid[i] = i;
+  c.eE[i] = 0.f;
+  c.epos_of_pid[i] = i;
+  SegState &sg = c.seg[s];
+  if (id[i] == sg.mb_id) atomicMin(&sg.first_mb, i - sg.off);
+}
+
+// ---------------------------------------------------------------- plans
+__device__ int get_pass(const Ctx &c, int s, int *v)
+{
+  const SegState &sg = c.seg[s];
+  const bool act = sg.status == SEG_ACTIVE;
+  v[0] = act ? sg.ntree : 0;
+  v[1] = act ? (sg.ntree + kChunk - 1) / kChunk : 0;
+  v[2] = act ? (sg.tgt_mode == 1 ? sg.coh_n : sg.ntgt) : 0;
+  v[3] = sg.ub_hi - sg.ub_lo;
+  return 0;
+}
+__device__ int get_bound(const Ctx &c, int s, int *v)
+{
+  const bool act = c.seg[s].status == SEG_ACTIVE;
+  const int nb = act ? c.part_info[8 * s + 7] : 0;
+  v[0] = (nb + kChunk - 1) / kChunk;
+  v[1] = v[2] = v[3] = 0;
+  return 0;
+}
+__device__ int get_final(const Ctx &c, int s, int *v)
+{
+  const SegState &sg = c.seg[s];
+  const bool conv = sg.status == SEG_CONVERGED || sg.status == SEG_FAILED;
+  const int nb = conv ? sg.nbound : 0;
+  v[0] = (nb + kChunk - 1) / kChunk;
+  v[1] = nb;  // bound block to sort
+  v[2] = sg.refine ? 1 : 0;
+  v[3] = 0;
+  return 0;
+}
+__device__ int get_refine(const Ctx &c, int s, int *v)
+{
+  const SegState &sg = c.seg[s];
+  v[0] = sg.refine ? (int)min((long long)sg.nbound, c.P.maxsample) : 0;
+  v[1] = v[2] = v[3] = 0;
+  return 0;
+}
+
+__global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode)
+{
+  __shared__ int tot[4];
+  __shared__ int nact;
+  if (threadIdx.x == 0) nact = 0;
+  __syncthreads();
+  if (mode == 0) {
+    int cnt = 0;
+    for (int s = threadIdx.x; s < c.S; s += kPlanThreads) cnt += c.seg[s].status == SEG_ACTIVE;
+    atomicAdd(&nact, cnt);
+    plan_scan4(c.S, get_pass, c, c.tree_base, c.tchunk_base, c.tgt_base, c.ub_base, tot);
+    if (threadIdx.x == 0) {
+      c.plan->nactive = nact;
+      c.plan->ntree_total = tot[0];
+      c.plan->nchunks_tree = tot[1];
+      c.plan->ntgt_total = tot[2];
+      c.plan->nsort_total = tot[3];
+      c.plan->max_levels = 0;
+    }
+  } else if (mode == 1) {
+    plan_scan4(c.S, get_bound, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
+    if (threadIdx.x == 0) c.plan->nchunks_bound = tot[0];
+  } else if (mode == 2) {
+    plan_scan4(c.S, get_final, c, c.bchunk_base, c.ub_base, nullptr, nullptr, tot);
+    if (threadIdx.x == 0) {
+      c.plan->nchunks_bound = tot[0];
+      c.plan->nsort_total = tot[1];
+      c.plan->nrefine = tot[2];
+    }
+  } else {
+    plan_scan4(c.S, get_refine, c, c.ub_base, nullptr, nullptr, nullptr, tot);
+    if (threadIdx.x == 0) c.plan->nsort_total = tot[0];
+  }
+}
+
+// ---------------------------------------------------------------- partition
+// part_info[8s+]: 0 nPos, 1 nNeg, 2 firstF, 3 firstG, 4 m_b, 5 m_f, 6 void, 7 Nbound
+__global__ void __launch_bounds__(kLB) k_part_codes(Ctx c)
+{
+  const int p = blockIdx.x * kLB + threadIdx.x;
+  if (p > c.N) return;
+  if (p == c.N) {
+    c.pcode[p] = 0;
+    return;
+  }
+  const int s = c.pseg[p];
+  const SegState &sg = c.seg[s];
+  const int l = p - sg.off;
+  long long code = 0;
+  if (sg.status == SEG_ACTIVE && l >= 1 && l < sg.nlast) {
+    const float e = c.eE[p];
+    code = (e < 0.f ? (1ll << 32) : 0ll) | (e > 0.f ? 1ll : 0ll);
+  }
+  c.pcode[p] = code;
+  if (l == 0) {
+    c.part_info[8 * s + 2] = 0x7fffffff;
+    c.part_info[8 * s + 3] = 0x7fffffff;
+  }
+}
+
+__device__ __forceinline__ int lo32(long long x) { return (int)(x & 0xffffffffll); }
+__device__ __forceinline__ int hi32(long long x) { return (int)(x >> 32); }
+
+__global__ void __launch_bounds__(kLB) k_part_pq(Ctx c)
+{
+  const int p = blockIdx.x * kLB + threadIdx.x;
+  if (p >= c.N) return;
+  const int s = c.pseg[p];
+  const SegState &sg = c.seg[s];
+  const int l = p - sg.off;
+  if (sg.status != SEG_ACTIVE || sg.nlast < 2) return;
+  const long long x1 = c.pX[sg.off + 1], xe = c.pX[sg.off + sg.nlast];
+  if (l == 0) {
+    c.part_info[8 * s + 0] = lo32(xe - x1);
+    c.part_info[8 * s + 1] = hi32(xe - x1);
+  }
+  if (l < 1 || l >= sg.nlast) return;
+  const float e = c.eE[p];
+  if (e > 0.f) c.Pk[sg.off + lo32(c.pX[p] - x1)] = l;
+  if (e < 0.f) c.Qk[sg.off + hi32(xe - c.pX[p]) - 1] = l;
+}
+
+__global__ void __launch_bounds__(kLB) k_part_fg(Ctx c)
+{
+  const int p = blockIdx.x * kLB + threadIdx.x;
+  if (p >= c.N) return;
+  const int s = c.pseg[p];
+  const SegState &sg = c.seg[s];
+  const int l = p - sg.off;
+  if (sg.status != SEG_ACTIVE || sg.nlast < 2 || l < 1 || l >= sg.nlast) return;
+  if (!(c.eE[p] > 0.f)) return;
+  const int k = lo32(c.pX[p] - c.pX[sg.off + 1]) + 1;
+  const int nPos = c.part_info[8 * s + 0], nNeg = c.part_info[8 * s + 1];
+  const int mn = min(nPos, nNeg);
+  if (k > mn) return;
+  const int Pk = l, Qk = c.Qk[sg.off + k - 1];
+  if (Pk >= Qk) atomicMin(&c.part_info[8 * s + 2], k);
+  if (k + 1 > nNeg || Pk >= c.Qk[sg.off + k]) atomicMin(&c.part_info[8 * s + 3], k);
+}
+
+__global__ void k_part_seg(Ctx c)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= c.S) return;
+  const SegState &sg = c.seg[s];
+  if (sg.status != SEG_ACTIVE) return;
+  int *pi = c.part_info + 8 * s;
+  const float e0 = c.eE[sg.off];
+  if (sg.nlast < 2) {
+    pi[4] = pi[5] = pi[6] = 0;
+    pi[7] = sg.nlast == 1 ? (e0 < 0.f) : 0;
+    return;
+  }
+  const int nPos = pi[0], nNeg = pi[1], mn = min(nPos, nNeg);
+  const int F = min(pi[2], mn + 1) - 1;
+  const int G = min(pi[3] - 1, F);
+  int mb = 0, mf = 0, vd = 0;
+  if (nNeg > 0) {
+    mb = 1 + G;
+    mf = G + (G + 1 <= F ? 1 : 0);
+    vd = (mf == mb) ? c.Pk[sg.off + mf - 1] : c.Qk[sg.off + mb - 1];
+  }
+  pi[4] = mb;
+  pi[5] = mf;
+  pi[6] = vd;
+  pi[7] = vd + (e0 < 0.f);
+}
+
+__global__ void __launch_bounds__(kLB) k_part_gather(Ctx c)
+{
+  const int p = blockIdx.x * kLB + threadIdx.x;
+  if (p >= c.N) return;
+  const int s = c.pseg[p];
+  const SegState &sg = c.seg[s];
+  const int l = p - sg.off;
+  if (sg.status != SEG_ACTIVE || l >= sg.nlast) return;
+  int src = l;
+  if (sg.nlast >= 2) {
+    const int *pi = c.part_info + 8 * s;
+    const int nNeg = pi[1], mb = pi[4], mf = pi[5], vd = pi[6];
+    const float e = c.eE[p];
+    if (l == vd) {
+      src = 0;
+    } else if (l == 0) {
+      src = nNeg >= 1 ? c.Qk[sg.off] : 0;
+    } else if (e < 0.f) {
+      const int kq = hi32(c.pX[sg.off + sg.nlast] - c.pX[p]);
+      if (kq <= mf) src = c.Pk[sg.off + kq - 1];
+    } else if (e > 0.f) {
+      const int kp = lo32(c.pX[p] - c.pX[sg.off + 1]) + 1;
+      if (kp <= mb - 1) src = c.Qk[sg.off + kp];
+    }
+  }
+  c.epid2[p] = c.epid[sg.off + src];
+  c.eE2[p] = c.eE[sg.off + src];
+}
+
+__global__ void __launch_bounds__(kLB) k_part_copyback(Ctx c)
+{
+  const int p = blockIdx.x * kLB + threadIdx.x;
+  if (p >= c.N) return;
+  const SegState &sg = c.seg[c.pseg[p]];
+  if (sg.status != SEG_ACTIVE || p - sg.off >= sg.nlast) return;
+  const int q = c.epid2[p];
+  c.epid[p] = q;
+  c.eE[p] = c.eE2[p];
+  c.epos_of_pid[q] = p;
+}
+
+// ---------------------------------------------------------------- averages
+__global__ void __launch_bounds__(kLB) k_avg_chunks(Ctx c)
+{
+  const int b = blockIdx.x;
+  if (b >= c.bchunk_base[c.S]) return;
+  const int s = upper_bound_i(c.bchunk_base, c.S + 1, b) - 1;
+  const SegState &sg = c.seg[s];
+  const int nb = c.part_info[8 * s + 7];
+  const int ci = b - c.bchunk_base[s];
+  const int lo = ci * kChunk, hi = min(lo + kChunk, nb);
+  const float4 o = c.pm[c.epid[sg.off]];
+  const double ox = o.x, oy = o.y, oz = o.z;
+  double v[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int p = lo + threadIdx.x; p < hi; p += kLB) {
+    const int pid = c.epid[sg.off + p];
+    const float4 a = c.pm[pid];
+    const float4 u = c.vel[pid];
+    const float m = a.w;
+    v[0] += (double)m;
+    v[1] += (double)fmul(u.x, m);
+    v[2] += (double)fmul(u.y, m);
+    v[3] += (double)fmul(u.z, m);
+    if (c.P.periodic) {
+      v[4] += dmul(nearest_d(dsub((double)a.x, ox), c.P), (double)m);
+      v[5] += dmul(nearest_d(dsub((double)a.y, oy), c.P), (double)m);
+      v[6] += dmul(nearest_d(dsub((double)a.z, oz), c.P), (double)m);
+    } else {
+      v[4] += (double)fmul(a.x, m);
+      v[5] += (double)fmul(a.y, m);
+      v[6] += (double)fmul(a.z, m);
+    }
+  }
+  block_sum<7>(v, c.chunk_sums + (size_t)b * kSums);
+}
+
+// ---------------------------------------------------------------- control
+__global__ void k_control(Ctx c, int max_passes)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= c.S) return;
+  SegState &sg = c.seg[s];
+  if (sg.status != SEG_ACTIVE) return;
+  const DevParams &P = c.P;
+  const int nb = c.part_info[8 * s + 7];
+  const int nl = sg.nlast;
+  sg.passes++;
+  sg.evals += sg.ntgt;
+  if (sg.tgt_mode == 0) sg.coh_n = sg.ntgt;
+  if (nb < P.minpart) {  // disruption (src/subhalo_unbind.cpp:361-379)
+    sg.status = SEG_DISRUPTED;
+    sg.e0 = c.eE[sg.off];
+    sg.nbound = 1;
+    sg.nlast = 1;
+    for (int j = 0; j < 3; j++) {
+      sg.ref_pos[j] = sg.mb_pos[j];
+      sg.ref_vel[j] = sg.mb_vel[j];
+    }
+    const int k = sg.first_mb < sg.n ? sg.first_mb : 0;
+    sg.mbound = c.pm[sg.off + k].w;
+    sg.ub_lo = sg.ub_hi = 0;
+    return;
+  }
+  sg.ub_lo = nb;
+  sg.ub_hi = nl;
+  const int ndiff = nl - nb;
+  if (ndiff < nb && (P.maxsample <= 0 || ndiff < P.maxsample)) {  // :383-392
+    sg.corr = 1;
+    for (int j = 0; j < 3; j++) {
+      sg.old_pos[j] = sg.ref_pos[j];
+      sg.old_vel[j] = sg.ref_vel[j];
+    }
+  }
+  if (nb == 1) {  // AverageVelocity / AveragePosition with one particle
+    const int pid = c.epid[sg.off];
+    const float4 a = c.pm[pid], u = c.vel[pid];
+    sg.mbound = a.w;
+    sg.ref_vel[0] = u.x;
+    sg.ref_vel[1] = u.y;
+    sg.ref_vel[2] = u.z;
+    sg.ref_pos[0] = a.x;
+    sg.ref_pos[1] = a.y;
+    sg.ref_pos[2] = a.z;
+  } else if (nb > 1) {
+    double v[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int b = c.bchunk_base[s]; b < c.bchunk_base[s + 1]; b++)
+      for (int k = 0; k < 7; k++) v[k] += c.chunk_sums[(size_t)b * kSums + k];
+    const double msum = v[0];
+    sg.mbound = (float)msum;
+    for (int j = 0; j < 3; j++) sg.ref_vel[j] = __double2float_rn(ddiv(v[1 + j], msum));
+    const float4 o = c.pm[c.epid[sg.off]];
+    const double org[3] = {o.x, o.y, o.z};
+    for (int j = 0; j < 3; j++) {
+      double x = ddiv(v[4 + j], msum);
+      if (P.periodic) x = dadd(x, org[j]);
+      sg.ref_pos[j] = __double2float_rn(x);
+    }
+  } else {
+    sg.mbound = 0.f;
+  }
+  if (__int2float_rn(nb) >= fmul(__int2float_rn(nl), P.prec)) {  // :395
+    sg.status = SEG_CONVERGED;
+    sg.nbound = nb;
+    sg.refine = P.refine && nb > P.maxsample;  // :406-407
+    return;
+  }
+  sg.nbound = nb;
+  if (sg.corr) {  // correction pass over the removed block (:312-330)
+    sg.mode = MODE_CORRECTION;
+    sg.t0 = nb;
+    sg.ntree = nl - nb;
+    sg.ntgt = nb;
+    sg.mfac = 1.f;
+    relvel(sg.old_pos, sg.old_vel, sg.ref_pos, sg.ref_vel, sg.dV, P);
+    sg.dK = __double2float_rn(dmul(0.5, (double)vdot(sg.dV, sg.dV)));
+    sg.tgt_mode = sg.coh_n > 0 ? 1 : 2;
+  } else {  // full pass (:331-356)
+    sg.mode = MODE_FULL;
+    sg.t0 = 0;
+    sg.ntgt = nb;
+    if (P.maxsample > 0 && nb > P.maxsample) {
+      sg.ntree = (int)P.maxsample;
+      sg.mfac = __fdiv_rn(__int2float_rn(nb), (float)P.maxsample);
+      sg.tgt_mode = 2;
+    } else {
+      sg.ntree = nb;
+      sg.mfac = 1.f;
+      sg.tgt_mode = 0;
+    }
+  }
+  sg.nlast = nb;
+  if (sg.passes >= max_passes) sg.status = SEG_FAILED;
+}
+
+// ---------------------------------------------------------------- block sorts
+// which 0: [ub_lo, ub_hi) of every subhalo; which 1: [0, nbound) of converged.
+__device__ __forceinline__ bool block_of(const SegState &sg, int which, int &lo, int &hi,
+                                         long long c_maxsample)
+{
+  if (which == 0) {
+    lo = sg.ub_lo;
+    hi = sg.ub_hi;
+  } else if (which == 2) {
+    lo = 0;
+    hi = sg.refine ? (int)min((long long)sg.nbound, c_maxsample) : 0;
+  } else {
+    lo = 0;
+    hi = (sg.status == SEG_CONVERGED || sg.status == SEG_FAILED) ? sg.nbound : 0;
+  }
+  return hi > lo;
+}
+
+__global__ void __launch_bounds__(kLB) k_blk_gather(Ctx c, int which)
+{
+  const int p = blockIdx.x * kLB + threadIdx.x;
+  if (p >= c.N) return;
+  const int s = c.pseg[p];
+  const SegState &sg = c.seg[s];
+  int lo, hi;
+  if (!block_of(sg, which, lo, hi, c.P.maxsample)) return;
+  const int l = p - sg.off;
+  if (l < lo || l >= hi) return;
+  const int e = c.ub_base[s] + (l - lo);
+  c.sb.hi_a[e] = (unsigned)s;
+  c.sb.lo_a[e] = (unsigned long long)float_key(which == 2 ? c.eR[p] : c.eE[p]) << 32;
+  c.sb.val_a[e] = p;
+}
+
+__global__ void __launch_bounds__(kLB) k_blk_scatter(Ctx c, int which, int total)
+{
+  const int e = blockIdx.x * kLB + threadIdx.x;
+  if (e >= total) return;
+  const int s = c.sb.hi_a[e];
+  const SegState &sg = c.seg[s];
+  int lo, hi;
+  block_of(sg, which, lo, hi, c.P.maxsample);
+  const int dst = sg.off + lo + (e - c.ub_base[s]);
+  const int src = c.sb.val_a[e];
+  c.epid2[dst] = c.epid[src];
+  c.eE2[dst] = c.eE[src];
+}
+
+__global__ void __launch_bounds__(kLB) k_blk_copyback(Ctx c, int which, int total)
+{
+  const int e = blockIdx.x * kLB + threadIdx.x;
+  if (e >= total) return;
+  const int s = c.sb.hi_a[e];
+  SegState &sg = c.seg[s];
+  int lo, hi;
+  block_of(sg, which, lo, hi, c.P.maxsample);
+  const int dst = sg.off + lo + (e - c.ub_base[s]);
+  const int q = c.epid2[dst];
+  c.epid[dst] = q;
+  c.eE[dst] = c.eE2[dst];
+  c.epos_of_pid[q] = dst;
+}
+
+// RefineBindingEnergyOrder (src/subhalo_unbind.cpp:234-262): one more full
+// pass over the first MaxSampleSize bound particles with their own masses;
+// energies go to eR and only reorder the list (its stored energies stay).
+__global__ void k_refine_mode(Ctx c, int enter)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= c.S) return;
+  SegState &sg = c.seg[s];
+  if (!sg.refine) return;
+  if (enter) {
+    sg.status = SEG_ACTIVE;
+    sg.mode = MODE_REFINE;
+    sg.t0 = 0;
+    sg.ntree = (int)min((long long)sg.nbound, c.P.maxsample);
+    sg.ntgt = sg.ntree;
+    sg.mfac = 1.f;
+    sg.tgt_mode = 0;
+    sg.evals += sg.ntgt;
+  } else {
+    sg.status = SEG_CONVERGED;
+  }
+}
+
+__global__ void k_blk_clear(Ctx c)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= c.S) return;
+  c.seg[s].ub_lo = c.seg[s].ub_hi = 0;
+}
+
+// ---------------------------------------------------------------- finalize
+__global__ void __launch_bounds__(kLB) k_kin_chunks(Ctx c)
+{
+  const int b = blockIdx.x;
+  if (b >= c.bchunk_base[c.S]) return;
+  const int s = upper_bound_i(c.bchunk_base, c.S + 1, b) - 1;
+  const SegState &sg = c.seg[s];
+  const DevParams &P = c.P;
+  const int nb = sg.nbound;
+  const int ci = b - c.bchunk_base[s];
+  const int lo = ci * kChunk, hi = min(lo + kChunk, nb);
+  double v[18];
+  for (int k = 0; k < 18; k++) v[k] = 0.;
+  for (int p = lo + threadIdx.x; p < hi; p += kLB) {
+    const int pid = c.epid[sg.off + p];
+    const float4 a = c.pm[pid], u = c.vel[pid];
+    const float m = a.w;
+    const float x[3] = {a.x, a.y, a.z}, w[3] = {u.x, u.y, u.z};
+    v[0] += (double)fmul(c.eE[sg.off + p], m);
+    double dx[3], dv[3];
+    for (int j = 0; j < 3; j++) {
+      dx[j] = (double)fsub(x[j], sg.ref_pos[j]);
+      if (P.periodic) dx[j] = nearest_d(dx[j], P);
+      dx[j] = dmul(dx[j], (double)P.a);
+      dv[j] = dadd((double)fsub(w[j], sg.ref_vel[j]), dmul((double)P.Hz, dx[j]));
+      v[1] += dmul(dmul(dv[j], dv[j]), (double)m);
+    }
+    v[2] += dmul(dsub(dmul(dx[1], dv[2]), dmul(dx[2], dv[1])), (double)m);
+    v[3] += dmul(dsub(dmul(dx[2], dv[0]), dmul(dx[0], dv[2])), (double)m);
+    v[4] += dmul(dsub(dmul(dx[0], dv[1]), dmul(dx[1], dv[0])), (double)m);
+    v[5] += (double)m;
+    const int t = c.type ? c.type[pid] : 1;
+    const bool skip = (nb <= 100 && c.id[pid] == -1) || t < 0 || t > 5;
+    if (!skip) {
+      v[6 + t] += 1.0;
+      v[12 + t] += (double)m;
+    }
+  }
+  block_sum<18>(v, c.chunk_sums + (size_t)b * kSums);
+}
+
+__global__ void k_final_seg(Ctx c, hbtu_result *res)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= c.S) return;
+  const SegState &sg = c.seg[s];
+  const DevParams &P = c.P;
+  hbtu_result r;
+  memset(&r, 0, sizeof(r));
+  r.too_few = sg.n < P.minpart;
+  r.iterations = sg.passes;
+  r.evaluations = sg.evals;
+  r.interactions = sg.interactions;
+  for (int j = 0; j < 3; j++) {
+    r.ref_pos[j] = sg.ref_pos[j];
+    r.ref_vel[j] = sg.ref_vel[j];
+    r.mostbound_pos[j] = sg.mb_pos[j];
+    r.mostbound_vel[j] = sg.mb_vel[j];
+  }
+  if (sg.status == SEG_TRIVIAL) {  // src/subhalo_unbind.cpp:275-293 + CountParticles
+    r.nbound = sg.n;
+    if (sg.n == 1) {
+      const int t = c.type ? c.type[sg.off] : 1;
+      const float m = c.pm[sg.off].w;
+      if (t >= 0 && t <= 5) {
+        r.nbound_type[t] = 1;
+        r.mbound_type[t] = m;
+      }
+      float acc = 0.f;
+      for (int k = 0; k < 6; k++) acc = fadd(acc, r.mbound_type[k]);
+      r.mbound = acc;
+    }
+  } else if (sg.status == SEG_DISRUPTED) {
+    r.disrupted = 1;
+    r.nbound = 1;
+    r.mbound = sg.mbound;
+    const int k = sg.first_mb < sg.n ? sg.first_mb : 0;
+    const int t = c.type ? c.type[sg.off + k] : 1;
+    const bool skip = c.id[sg.off + k] == -1 || t < 0 || t > 5;
+    if (!skip) {
+      r.nbound_type[t] = 1;
+      r.mbound_type[t] = c.pm[sg.off + k].w;
+    }
+  } else {
+    r.converged = sg.status == SEG_CONVERGED;
+    if (sg.status == SEG_FAILED) r.status = HBTU_ERR_NOT_CONVERGED;
+    r.nbound = sg.nbound;
+    r.mbound = sg.mbound;
+    if (sg.nbound > 0) {
+      const int pid = c.epid[sg.off];
+      const float4 a = c.pm[pid], u = c.vel[pid];
+      r.mostbound_pos[0] = a.x;
+      r.mostbound_pos[1] = a.y;
+      r.mostbound_pos[2] = a.z;
+      r.mostbound_vel[0] = u.x;
+      r.mostbound_vel[1] = u.y;
+      r.mostbound_vel[2] = u.z;
+    }
+    double v[18];
+    for (int k = 0; k < 18; k++) v[k] = 0.;
+    for (int b = c.bchunk_base[s]; b < c.bchunk_base[s + 1]; b++)
+      for (int k = 0; k < 18; k++) v[k] += c.chunk_sums[(size_t)b * kSums + k];
+    if (sg.nbound > 1) {
+      const double M = v[5];
+      const double E = ddiv(v[0], M);
+      const double K = dmul(v[1], ddiv(0.5, M));
+      r.specific_potential = __double2float_rn(dsub(E, K));
+      r.specific_kinetic = __double2float_rn(K);
+      for (int j = 0; j < 3; j++) r.specific_angmom[j] = __double2float_rn(ddiv(v[2 + j], M));
+    }
+    for (int t = 0; t < 6; t++) {
+      r.nbound_type[t] = (int64_t)v[6 + t];
+      r.mbound_type[t] = (float)v[12 + t];
+    }
+  }
+  res[s] = r;
+}
+
+__global__ void __launch_bounds__(kLB) k_final_out(Ctx c, int64_t *order, float *energy)
+{
+  const int p = blockIdx.x * kLB + threadIdx.x;
+  if (p >= c.N) return;
+  const SegState &sg = c.seg[c.pseg[p]];
+  const int l = p - sg.off;
+  if (sg.status == SEG_TRIVIAL) {
+    order[p] = l;
+    energy[p] = 0.f;
+  } else if (sg.status == SEG_DISRUPTED) {
+    const int k = sg.first_mb < sg.n ? sg.first_mb : 0;
+    order[p] = l == 0 ? k : (l == k ? 0 : l);
+    energy[p] = l == 0 ? sg.e0 : __int_as_float(0x7fc00000);
+  } else {
+    order[p] = c.epid[p] - sg.off;
+    energy[p] = c.eE[p];
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers
+void launch_init(Ctx &c, const float *pos, const float *vel, const float *mass,
+                 const long long *id)
+{
+  k_init<<<nblk(c.N), kLB, 0, c.st>>>(c, pos, vel, mass, id);
+  HBTU_LAUNCHED();
+}
+
+void launch_plan(Ctx &c, int mode)
+{
+  k_plan<<<1, kPlanThreads, 0, c.st>>>(c, mode);
+  HBTU_LAUNCHED();
+}
+
+void launch_partition(Ctx &c)
+{
+  k_part_codes<<<nblk(c.N + 1), kLB, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+  exclusive_scan_i64(c.pcode, c.pX, c.N + 1, c.scan_tmp, c.st);
+  k_part_pq<<<nblk(c.N), kLB, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+  k_part_fg<<<nblk(c.N), kLB, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+  k_part_seg<<<nblk(c.S, 128), 128, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+  k_part_gather<<<nblk(c.N), kLB, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+  k_part_copyback<<<nblk(c.N), kLB, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+}
+
+void launch_averages_control(Ctx &c, int max_passes)
+{
+  launch_plan(c, 1);
+  const int max_chunks = (c.N + kChunk - 1) / kChunk + c.S;
+  k_avg_chunks<<<max_chunks, kLB, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+  k_control<<<nblk(c.S, 128), 128, 0, c.st>>>(c, max_passes);
+  HBTU_LAUNCHED();
+}
+
+void launch_block_sort(Ctx &c, int total, int which)
+{
+  if (total > 0) {
+    k_blk_gather<<<nblk(c.N), kLB, 0, c.st>>>(c, which);
+    HBTU_LAUNCHED();
+    int words[8], shifts[8], np = 0;
+    for (int p = 0; p < 4; p++) {
+      words[np] = 0;
+      shifts[np++] = 32 + 8 * p;
+    }
+    int sbits = 0;
+    while ((1 << sbits) < c.S) sbits++;
+    for (int p = 0; p < (sbits + 7) / 8; p++) {
+      words[np] = 1;
+      shifts[np++] = 8 * p;
+    }
+    radix_sort(c.sb, total, words, shifts, np, c.st);
+    k_blk_scatter<<<nblk(total), kLB, 0, c.st>>>(c, which, total);
+    HBTU_LAUNCHED();
+    k_blk_copyback<<<nblk(total), kLB, 0, c.st>>>(c, which, total);
+    HBTU_LAUNCHED();
+  }
+  if (which == 0) {
+    k_blk_clear<<<nblk(c.S, 128), 128, 0, c.st>>>(c);
+    HBTU_LAUNCHED();
+  }
+}
+
+void launch_refine_mode(Ctx &c, int enter)
+{
+  k_refine_mode<<<nblk(c.S, 128), 128, 0, c.st>>>(c, enter);
+  HBTU_LAUNCHED();
+}
+
+void launch_finalize(Ctx &c, int64_t *order_out, float *energy_out, hbtu_result *res_dev)
+{
+  const int max_chunks = (c.N + kChunk - 1) / kChunk + c.S;
+  k_kin_chunks<<<max_chunks, kLB, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+  k_final_seg<<<nblk(c.S, 128), 128, 0, c.st>>>(c, res_dev);
+  HBTU_LAUNCHED();
+  if (c.N > 0) {
+    k_final_out<<<nblk(c.N), kLB, 0, c.st>>>(c, order_out, energy_out);
+    HBTU_LAUNCHED();
+  }
+}
+
+}  // namespace hbtu

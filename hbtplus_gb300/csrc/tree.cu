@@ -1,0 +1,387 @@
+// tree.cu -- octree build for every active subhalo of a batch.
+//
+// Reproduces the cells of the reference's OctTree_t::Build
+// (src/oct_tree.tpp:16-144) without its serial insertion:
+//   1. bounding cube per subhalo: centre = box midpoint, side = largest extent,
+//      in double on the float positions (tpp:30-51);
+//   2. octal key of each particle: the octant chosen at each level by the
+//      reference's own test x > centre with centres halved in double
+//      (tpp:67-95), down to the level whose side drops below
+//      TreeNodeResolution (below it the reference places particles in random
+//      octants, tpp:112-123; here such particles share one bucket cell);
+//   3. stable LSD radix sort by (subhalo, key): DFS order with octants 0..7,
+//      which is the reference's nextnode/sibling order
+//      (src/gravity_tree.cpp:48-77);
+//   4. Karras binary radix tree on the sorted keys, collapsed to the octree
+//      cells where a key prefix branches.  A cell with one child cell has the
+//      same mass and centre of mass as that child (exact in double), so the
+//      collapsed cell, given the smaller child's side, makes the same walk;
+//   5. DFS preorder numbering and skip pointers from prefix counts;
+//   6. bottom-up mass and centre of mass over each cell's children in octant
+//      order, in double, rounded to float per cell as the reference does
+//      (ProcessNode / FillNodeCenter, src/gravity_tree.cpp:18-46).
+#include "device_common.cuh"
+
+namespace hbtu {
+namespace {
+
+constexpr int kTB = 256;
+
+__global__ void __launch_bounds__(kTB) k_bbox_chunks(Ctx c)
+{
+  const int b = blockIdx.x;
+  const int total = c.tchunk_base[c.S];
+  if (b >= total) return;
+  const int s = upper_bound_i(c.tchunk_base, c.S + 1, b) - 1;
+  const SegState &sg = c.seg[s];
+  const int ci = b - c.tchunk_base[s];
+  const int lo = sg.t0 + ci * kChunk, hi = min(sg.t0 + (ci + 1) * kChunk, sg.t0 + sg.ntree);
+  float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int p = lo + threadIdx.x; p < hi; p += kTB) {
+    const float4 a = c.pm[c.epid[sg.off + p]];
+    mn[0] = fminf(mn[0], a.x);
+    mn[1] = fminf(mn[1], a.y);
+    mn[2] = fminf(mn[2], a.z);
+    mx[0] = fmaxf(mx[0], a.x);
+    mx[1] = fmaxf(mx[1], a.y);
+    mx[2] = fmaxf(mx[2], a.z);
+  }
+  __shared__ float sh[6][kTB / 32];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[j] = fminf(mn[j], __shfl_xor_sync(0xffffffffu, mn[j], o));
+      mx[j] = fmaxf(mx[j], __shfl_xor_sync(0xffffffffu, mx[j], o));
+    }
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+    for (int j = 0; j < 3; j++) {
+      sh[j][w] = mn[j];
+      sh[3 + j][w] = mx[j];
+    }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    const int j = threadIdx.x;
+    float v = sh[j][0];
+    for (int k = 1; k < kTB / 32; k++) v = j < 3 ? fminf(v, sh[j][k]) : fmaxf(v, sh[j][k]);
+    c.chunk_bbox[(size_t)b * 6 + j] = __float_as_uint(v);
+  }
+}
+
+// Root cube of each active subhalo (src/oct_tree.tpp:30-51) and its depth of
+// geometric subdivision: the first level whose side is below TreeNodeResolution
+// (the len halving rule of src/gravity_tree.cpp:37-40).
+__global__ void k_cube(Ctx c)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= c.S) return;
+  SegState &sg = c.seg[s];
+  if (sg.status != SEG_ACTIVE) return;
+  double xmin[3] = {0, 0, 0}, xmax[3] = {0, 0, 0};
+  const int b0 = c.tchunk_base[s], b1 = c.tchunk_base[s + 1];
+  for (int j = 0; j < 3; j++) {
+    float mn = INFINITY, mx = -INFINITY;
+    for (int b = b0; b < b1; b++) {
+      mn = fminf(mn, __uint_as_float(c.chunk_bbox[(size_t)b * 6 + j]));
+      mx = fmaxf(mx, __uint_as_float(c.chunk_bbox[(size_t)b * 6 + 3 + j]));
+    }
+    xmin[j] = mn;
+    xmax[j] = mx;
+  }
+  double Len = dsub(xmax[0], xmin[0]);
+  for (int j = 1; j < 3; j++) {
+    const double e = dsub(xmax[j], xmin[j]);
+    if (e > Len) Len = e;
+  }
+  for (int j = 0; j < 3; j++) sg.center[j] = dmul(0.5, dadd(xmax[j], xmin[j]));
+  if (b1 == b0) Len = 0.;
+  sg.len = Len;
+  int levels = 0;
+  double L = Len;
+  while (L >= (double)c.P.res && levels < kMaxLevels) {
+    L = dmul(L, 0.5);
+    levels++;
+  }
+  sg.levels = levels;
+  for (int j = 0; j < 3; j++) sg.fc[j] = sg.ref_pos[j];
+  atomicMax(&c.plan->max_levels, levels);
+}
+
+// Octal key: digit k (k = 1..levels) is the octant at depth k, found with the
+// reference's comparisons against centres halved in double.  Left-aligned.
+__global__ void __launch_bounds__(kTB) k_keys(Ctx c, int ntotal)
+{
+  const int e = blockIdx.x * kTB + threadIdx.x;
+  if (e >= ntotal) return;
+  const int s = upper_bound_i(c.tree_base, c.S + 1, e) - 1;
+  const SegState &sg = c.seg[s];
+  const int epos = sg.off + sg.t0 + (e - c.tree_base[s]);
+  const float4 a = c.pm[c.epid[epos]];
+  const float x[3] = {a.x, a.y, a.z};
+  double cen[3] = {sg.center[0], sg.center[1], sg.center[2]};
+  double lenhalf = dmul(0.5, sg.len);
+  unsigned long long key = 0;
+  for (int k = 0; k < sg.levels; k++) {
+    lenhalf = dmul(lenhalf, 0.5);
+    unsigned d = 0;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      if ((double)x[j] > cen[j]) {
+        cen[j] = dadd(cen[j], lenhalf);
+        d |= 1u << j;
+      } else {
+        cen[j] = dsub(cen[j], lenhalf);
+      }
+    }
+    key = (key << 3) | d;
+  }
+  if (sg.levels > 0) key <<= (64 - 3 * sg.levels);
+  c.sb.lo_a[e] = key;
+  c.sb.hi_a[e] = (unsigned)s;
+  c.sb.val_a[e] = epos;
+}
+
+__device__ __forceinline__ int kdelta(const unsigned long long *keys, int n, int i, int j)
+{
+  if (j < 0 || j >= n) return -1;
+  const unsigned long long a = keys[i], b = keys[j];
+  if (a != b) return __clzll(a ^ b);
+  return 64 + __clz((unsigned)(i ^ j));
+}
+
+// Karras (2012) binary radix tree over each subhalo's sorted keys.
+// Child codes: internal node -> its element index; leaf -> ~element index.
+__global__ void __launch_bounds__(kTB) k_karras(Ctx c, int ntotal)
+{
+  const int e = blockIdx.x * kTB + threadIdx.x;
+  if (e >= ntotal) return;
+  const int s = c.sb.hi_a[e];
+  const int base = c.tree_base[s], n = c.tree_base[s + 1] - base;
+  const int i = e - base;
+  if (i >= n - 1) return;
+  const unsigned long long *keys = c.sb.lo_a + base;
+  const int d = (kdelta(keys, n, i, i + 1) - kdelta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = kdelta(keys, n, i, i - d);
+  int lmax = 2;
+  while (kdelta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (kdelta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = i + l * d;
+  const int dn = kdelta(keys, n, i, j);
+  int sp = 0, t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (kdelta(keys, n, i, i + (sp + t) * d) > dn) sp += t;
+  } while (t > 1);
+  const int gamma = i + sp * d + min(d, 0);
+  const int first = min(i, j), last = max(i, j);
+  c.rfirst[e] = first;
+  c.rlast[e] = last;
+  c.dnode[e] = dn;
+  if (first == gamma) {
+    c.childL[e] = ~(base + gamma);
+    c.parentL[base + gamma] = e;
+  } else {
+    c.childL[e] = base + gamma;
+    c.parentI[base + gamma] = e;
+  }
+  if (last == gamma + 1) {
+    c.childR[e] = ~(base + gamma + 1);
+    c.parentL[base + gamma + 1] = e;
+  } else {
+    c.childR[e] = base + gamma + 1;
+    c.parentI[base + gamma + 1] = e;
+  }
+  if (i == 0) c.parentI[e] = -1;
+}
+
+__device__ __forceinline__ int oct_depth(int dn, int levels) { return min(dn / 3, levels); }
+
+// An internal node is an octree cell when its octal depth exceeds its
+// parent's (the root always is).  Record depth bits per first key.
+__global__ void __launch_bounds__(kTB) k_cells(Ctx c, int ntotal)
+{
+  const int e = blockIdx.x * kTB + threadIdx.x;
+  if (e >= ntotal) return;
+  const int s = c.sb.hi_a[e];
+  const int base = c.tree_base[s], n = c.tree_base[s + 1] - base;
+  if (e - base >= n - 1) {
+    c.iscell[e] = 0;
+    return;
+  }
+  const int L = c.seg[s].levels;
+  const int od = oct_depth(c.dnode[e], L);
+  const int p = c.parentI[e];
+  const int odp = p < 0 ? -1 : oct_depth(c.dnode[p], L);
+  const int cell = od > odp;
+  c.iscell[e] = cell;
+  if (cell) atomicOr(&c.mask[base + c.rfirst[e]], 1ull << od);
+}
+
+__global__ void __launch_bounds__(kTB) k_popc(Ctx c, int ntotal)
+{
+  const int e = blockIdx.x * kTB + threadIdx.x;
+  if (e > ntotal) return;
+  c.pcode[e] = e < ntotal ? __popcll(c.mask[e]) : 0;
+}
+
+__device__ __forceinline__ float4 make_rel(float4 a, const float fc[3], const DevParams &P)
+{
+  return make_float4(rel_coord(a.x, fc[0], P), rel_coord(a.y, fc[1], P), rel_coord(a.z, fc[2], P),
+                     a.w);
+}
+
+// Particle leaves: preorder index = j + #cells starting at or before key j.
+__global__ void __launch_bounds__(kTB) k_leaves(Ctx c, int ntotal)
+{
+  const int e = blockIdx.x * kTB + threadIdx.x;
+  if (e >= ntotal) return;
+  const int s = c.sb.hi_a[e];
+  SegState &sg = c.seg[s];
+  const int base = c.tree_base[s], n = c.tree_base[s + 1] - base;
+  const int j = e - base;
+  const int nb = 2 * base;
+  const float4 a0 = c.pm[c.epid[c.sb.val_a[e]]];
+  const float4 a = make_float4(a0.x, a0.y, a0.z, fmul(a0.w, sg.mfac));
+  if (n == 1) {  // a root cell of side 0 holding the particle (tpp:56-102 with one particle)
+    const float4 r = make_rel(a, sg.fc, c.P);
+    c.nd_abs[nb] = a;
+    c.nd_rel[nb] = r;
+    c.nd_len2[nb] = fmul((float)sg.len, (float)sg.len);
+    c.nd_skip[nb] = nb + 2;
+    c.nd_abs[nb + 1] = a;
+    c.nd_rel[nb + 1] = r;
+    c.nd_len2[nb + 1] = 0.f;
+    c.nd_skip[nb + 1] = nb + 2;
+    sg.nnodes = 2;
+    return;
+  }
+  const long long xb = c.X[base];
+  const int idx = j + (int)(c.X[e + 1] - xb);
+  c.nd_abs[nb + idx] = a;
+  c.nd_rel[nb + idx] = make_rel(a, sg.fc, c.P);
+  c.nd_len2[nb + idx] = 0.f;
+  c.nd_skip[nb + idx] = nb + idx + 1;
+  if (j == 0) sg.nnodes = n + (int)(c.X[base + n] - xb);
+}
+
+// Cells: preorder index, skip pointer, side (len*len in float), parent cell.
+__global__ void __launch_bounds__(kTB) k_cellnodes(Ctx c, int ntotal)
+{
+  const int e = blockIdx.x * kTB + threadIdx.x;
+  if (e >= ntotal || !c.iscell[e]) return;
+  const int s = c.sb.hi_a[e];
+  const SegState &sg = c.seg[s];
+  const int base = c.tree_base[s];
+  const int nb = 2 * base;
+  const int od = oct_depth(c.dnode[e], sg.levels);
+  const int lo = c.rfirst[e], hi = c.rlast[e];
+  const unsigned long long m = c.mask[base + lo];
+  const int rank = __popcll(m & ((1ull << od) - 1ull));
+  const long long xb = c.X[base];
+  const int idx = lo + (int)(c.X[base + lo] - xb) + rank;
+  const int skip = hi + 1 + (int)(c.X[base + hi + 1] - xb);
+  double len = sg.len;
+  for (int k = 0; k < od; k++)
+    if (len >= (double)c.P.res) len = dmul(len, 0.5);
+  const float lf = (float)len;
+  c.nd_len2[nb + idx] = fmul(lf, lf);
+  c.nd_skip[nb + idx] = nb + skip;
+  c.cidx[e] = nb + idx;
+  c.cskip[e] = nb + skip;
+  int p = c.parentI[e];
+  for (int guard = 0; p >= 0 && !c.iscell[p] && guard < 256; guard++) p = c.parentI[p];
+  if (p >= 0 && !c.iscell[p]) p = -1;  // malformed tree: never climb past it
+  c.pcell[e] = p;
+  if (p >= 0) atomicAdd(&c.pending[p], 1);
+}
+
+// Bottom-up moments: a cell is summed once all its child cells are, by the
+// thread that finished the last child (atomic countdown, no waiting).
+__global__ void __launch_bounds__(kTB) k_moments(Ctx c, int ntotal)
+{
+  int e = blockIdx.x * kTB + threadIdx.x;
+  if (e >= ntotal || !c.iscell[e] || c.pending0[e] != 0) return;
+  const int s = c.sb.hi_a[e];
+  const SegState &sg = c.seg[s];
+  for (int level = 0; level <= 2 * kMaxLevels + 2; level++) {
+    const int idx = c.cidx[e], end = c.cskip[e];
+    double m = 0., cx = 0., cy = 0., cz = 0.;
+    for (int k = idx + 1; k < end;) {
+      const float4 a = __ldcg(&c.nd_abs[k]);
+      const double w = (double)a.w;
+      m = dadd(m, w);
+      cx = dadd(cx, dmul((double)a.x, w));
+      cy = dadd(cy, dmul((double)a.y, w));
+      cz = dadd(cz, dmul((double)a.z, w));
+      const int nk = c.nd_skip[k];
+      k = nk > k ? nk : end;  // skip pointers always move forward
+    }
+    const float4 r = make_float4(__double2float_rn(ddiv(cx, m)), __double2float_rn(ddiv(cy, m)),
+                                 __double2float_rn(ddiv(cz, m)), __double2float_rn(m));
+    __stcg(&c.nd_abs[idx], r);
+    c.nd_rel[idx] = make_rel(r, sg.fc, c.P);
+    __threadfence();
+    const int p = c.pcell[e];
+    if (p < 0) break;
+    if (atomicSub(&c.pending[p], 1) != 1) break;
+    __threadfence();
+    e = p;
+  }
+}
+
+inline unsigned nblk(long long n) { return (unsigned)((n + kTB - 1) / kTB); }
+
+}  // namespace
+
+void launch_bbox_cube(Ctx &c, int max_chunks)
+{
+  if (max_chunks > 0) k_bbox_chunks<<<max_chunks, kTB, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+  k_cube<<<(c.S + 127) / 128, 128, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+}
+
+void launch_tree_build(Ctx &c, const PassPlan &pl)
+{
+  const int n = pl.ntree_total;
+  if (n <= 0) return;
+  k_keys<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  HBTU_LAUNCHED();
+  // LSD passes: octal-key digits (top 3*levels bits), then subhalo index
+  int words[16], shifts[16], np = 0;
+  const int kbits = 3 * pl.max_levels;
+  const int kp = (kbits + 7) / 8;
+  for (int p = 0; p < kp; p++) {
+    words[np] = 0;
+    shifts[np++] = 64 - 8 * kp + 8 * p;
+  }
+  int sbits = 0;
+  while ((1 << sbits) < c.S) sbits++;
+  for (int p = 0; p < (sbits + 7) / 8; p++) {
+    words[np] = 1;
+    shifts[np++] = 8 * p;
+  }
+  radix_sort(c.sb, n, words, shifts, np, c.st);
+  HBTU_CUDA(cudaMemsetAsync(c.mask, 0, sizeof(unsigned long long) * (size_t)n, c.st));
+  HBTU_CUDA(cudaMemsetAsync(c.pending, 0, sizeof(int) * (size_t)n, c.st));
+  k_karras<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  HBTU_LAUNCHED();
+  k_cells<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  HBTU_LAUNCHED();
+  k_popc<<<nblk(n + 1), kTB, 0, c.st>>>(c, n);
+  HBTU_LAUNCHED();
+  exclusive_scan_i64(c.pcode, c.X, n + 1, c.scan_tmp, c.st);
+  k_leaves<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  HBTU_LAUNCHED();
+  k_cellnodes<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  HBTU_LAUNCHED();
+  HBTU_CUDA(cudaMemcpyAsync(c.pending0, c.pending, sizeof(int) * (size_t)n,
+                            cudaMemcpyDeviceToDevice, c.st));
+  k_moments<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  HBTU_LAUNCHED();
+}
+
+}  // namespace hbtu

@@ -1,0 +1,186 @@
+/* hbtu.h -- C ABI of the GB300 (sm_103a) subhalo-unbinding library.
+ *
+ * Drop-in replacement for HBT+'s unbinding step:
+ *   void Subhalo_t::Unbind(const Snapshot_t &epoch)
+ *     src/subhalo.h:111, src/subhalo_unbind.cpp:263-431
+ * and for the per-subhalo loops of its caller
+ *   void SubhaloSnapshot_t::RefineParticles()   src/subhalo_unbind.cpp:460-516
+ * (gather all subhaloes of one nesting level into one batch call).
+ *
+ * Plain C: no exceptions cross it, every call returns an hbtu_status, buffers
+ * are owned by the caller.  One handle = one CUDA stream and one device
+ * workspace; calls on different handles may run concurrently from different
+ * host threads; calls on one handle must not overlap.
+ */
+#ifndef HBTU_H
+#define HBTU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum hbtu_status {
+  HBTU_OK = 0,
+  HBTU_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size or parameter */
+  HBTU_ERR_CUDA = 2,             /* a CUDA runtime call failed (see hbtu_last_error) */
+  HBTU_ERR_OUT_OF_MEMORY = 3,    /* device workspace could not be allocated */
+  HBTU_ERR_NOT_CONVERGED = 4,    /* a subhalo hit max_passes (see hbtu_result.status) */
+  HBTU_ERR_NO_DEVICE = 5,        /* no CUDA device of compute capability 10.3 */
+  HBTU_ERR_TOO_LARGE = 6         /* more than HBTU_MAX_PARTICLES particles in one call */
+} hbtu_status;
+
+#define HBTU_MAX_PARTICLES ((int64_t)1 << 30)
+
+typedef enum hbtu_precision {
+  HBTU_PRECISION_FP32 = 0, /* walk in FP32 on coordinates relative to the subhalo,
+                              FP64 sums for frames and convergence (default) */
+  HBTU_PRECISION_FP64 = 1  /* walk in FP64 with the reference's operation order */
+} hbtu_precision;
+
+typedef enum hbtu_location { HBTU_HOST = 0, HBTU_DEVICE = 1 } hbtu_location;
+
+/* Unbinding parameters: the subset of HBT+'s Parameter_t read by Unbind
+ * (src/config_parser.h:22-123), the snapshot's cosmology and G.  Values are
+ * rounded to float (HBTReal) exactly as the reference stores them. */
+typedef struct hbtu_params {
+  double softening;            /* SofteningHalo (compulsory) */
+  double open_angle;           /* TreeNodeOpenAngle, default 0.45 */
+  double bound_mass_precision; /* BoundMassPrecision, default 0.995 */
+  int64_t min_num_part;        /* MinNumPartOfSub, default 20 */
+  int64_t max_sample_size;     /* MaxSampleSizeOfPotentialEstimate, default 1000; 0 = exact */
+  int32_t refine_mostbound;    /* RefineMostboundParticle, default 1 */
+  int32_t periodic;            /* PeriodicBoundaryOn, default 1 */
+  double box_size;             /* BoxSize */
+  double G;                    /* PhysicalConst::G = 43.0071*(MassInMsunh/1e10)/VelInKmS^2/LengthInMpch */
+  double hubble;               /* Cosmology.Hz of the snapshot (internal units) */
+  double scale_factor;         /* Cosmology.ScaleFactor of the snapshot */
+  int32_t precision;           /* hbtu_precision */
+  int32_t max_passes;          /* cap on loop passes per subhalo (0 = 10000) */
+  int32_t device;              /* CUDA device ordinal */
+  int32_t reserved;
+} hbtu_params;
+
+/* Per-subhalo state read by Unbind besides its particles. */
+typedef struct hbtu_state {
+  float ref_pos[3];       /* ComovingAveragePosition: initial frame */
+  float ref_vel[3];       /* PhysicalAverageVelocity: initial frame */
+  float mostbound_pos[3]; /* ComovingMostBoundPosition (restored on disruption) */
+  float mostbound_vel[3]; /* PhysicalMostBoundVelocity (restored on disruption) */
+  int64_t mostbound_id;   /* Id of the previous most-bound particle (Particles[0]
+                             before the sampling shuffle) */
+} hbtu_state;
+
+/* Per-subhalo outputs: the Subhalo_t members Unbind writes (src/subhalo.h:29-91). */
+typedef struct hbtu_result {
+  int64_t nbound;           /* Nbound */
+  float mbound;             /* Mbound */
+  float ref_pos[3];         /* ComovingAveragePosition */
+  float ref_vel[3];         /* PhysicalAverageVelocity */
+  float mostbound_pos[3];   /* ComovingMostBoundPosition */
+  float mostbound_vel[3];   /* PhysicalMostBoundVelocity */
+  float specific_potential; /* SpecificSelfPotentialEnergy */
+  float specific_kinetic;   /* SpecificSelfKineticEnergy */
+  float specific_angmom[3]; /* SpecificAngularMomentum */
+  int64_t nbound_type[6];   /* NboundType */
+  float mbound_type[6];     /* MboundType */
+  int32_t iterations;       /* passes of the unbinding loop */
+  int32_t disrupted;        /* the disruption branch ran: set SnapshotIndexOfDeath if alive */
+  int32_t converged;        /* converged: clear death (if dead) and sink (if trapped) */
+  int32_t too_few;          /* n < MinNumPartOfSub: set SnapshotIndexOfDeath if alive */
+  int64_t evaluations;      /* target potentials evaluated */
+  int64_t interactions;     /* tree-walk contributions summed */
+  int32_t status;           /* 0 ok, HBTU_ERR_NOT_CONVERGED if max_passes was hit */
+  int32_t reserved;
+} hbtu_result;
+
+/* Particle arrays of one call (n particles, or the concatenation of a batch).
+ * pos and vel hold 3 floats per particle (HBTxyz), like Particle_t. */
+typedef struct hbtu_particles {
+  const int64_t *id;   /* Particle_t::Id */
+  const float *pos;    /* Particle_t::ComovingPosition, 3n */
+  const float *vel;    /* Particle_t::PhysicalVelocity, 3n */
+  const float *mass;   /* Particle_t::Mass */
+  const int32_t *type; /* Particle_t::Type (0..5), may be NULL (all TypeDM) */
+  int32_t location;    /* hbtu_location of these arrays AND of the output arrays */
+  int32_t reserved;
+} hbtu_particles;
+
+typedef struct hbtu_handle hbtu_handle;
+
+/* Create a handle on params->device, with its own stream and workspace.
+ * Replaces the configuration read of Parameter_t::ParseConfigFile
+ * (src/config_parser.cpp:74-109) for the unbinding subset. */
+hbtu_status hbtu_create(const hbtu_params *params, hbtu_handle **out);
+hbtu_status hbtu_destroy(hbtu_handle *h);
+
+/* Replace the handle's stream by a caller-owned cudaStream_t (NULL: the
+ * handle's own stream). */
+hbtu_status hbtu_set_stream(hbtu_handle *h, void *cuda_stream);
+
+/* Unbind one subhalo: Subhalo_t::Unbind (src/subhalo_unbind.cpp:263-431).
+ *   p, n:       its particles; position 0 = the previous most-bound particle
+ *               (when sampling applies the caller has applied the reference's
+ *               random_shuffle first, src/subhalo_unbind.cpp:302)
+ *   st:         frame and most-bound record on entry (host memory)
+ *   order_out:  n int64; output position i holds input particle order_out[i]
+ *               (the permuted Particles vector)
+ *   energy_out: n float; binding energy at output position i; the first
+ *               nbound are Subhalo_t::Energies (SAVE_BINDING_ENERGY)
+ *   res:        one hbtu_result (same location as the particle arrays) */
+hbtu_status hbtu_unbind(hbtu_handle *h, const hbtu_particles *p, int64_t n,
+                        const hbtu_state *st, int64_t *order_out, float *energy_out,
+                        hbtu_result *res);
+
+/* Unbind nsub independent subhaloes in one device-resident loop: the
+ * per-subhalo Unbind calls of SubhaloSnapshot_t::RefineParticles
+ * (src/subhalo_unbind.cpp:471-513) for one nesting level.
+ *   offsets: nsub+1 int64 (host memory); subhalo s owns particles
+ *            [offsets[s], offsets[s+1]) of p
+ *   st:      nsub states (host memory)
+ *   order_out / energy_out: per particle, positions local to each subhalo
+ *   res:     nsub results (same location as the particle arrays) */
+hbtu_status hbtu_unbind_batch(hbtu_handle *h, const hbtu_particles *p, int64_t nsub,
+                              const int64_t *offsets, const hbtu_state *st, int64_t *order_out,
+                              float *energy_out, hbtu_result *res);
+
+/* One energy pass: a tree over all n particles and, for each,
+ * GravityTree_t::BindingEnergy (src/gravity_tree.cpp:166-175) with the
+ * self-term cancelled -- the first pass of the unbinding loop
+ * (src/subhalo_unbind.cpp:333-354).  potential_out (may be NULL) receives
+ * GravityTree_t::EvaluatePotential (src/gravity_tree.cpp:79-164). */
+hbtu_status hbtu_binding_energies(hbtu_handle *h, const hbtu_particles *p, int64_t n,
+                                  const float ref_pos[3], const float ref_vel[3],
+                                  float *energy_out, double *potential_out);
+
+/* Counters and device timings accumulated by a handle (tracing). */
+typedef struct hbtu_stats {
+  double total_ms;         /* device time of the unbinding calls, CUDA events on the handle's stream */
+  double tree_ms;          /* with timing on: octree builds (keys, sort, cells, moments) */
+  double walk_ms;          /* with timing on: the Barnes-Hut energy walks */
+  double loop_ms;          /* with timing on: partition, averages, control, energy sorts */
+  int64_t calls;           /* unbinding calls */
+  int64_t passes;          /* loop passes (all subhaloes of a call advance together) */
+  int64_t kernel_launches; /* CUDA kernels launched by the library */
+  int64_t walk_launches;   /* of which tree walks */
+  int64_t evaluations;     /* target potentials evaluated */
+  int64_t interactions;    /* tree-walk contributions summed */
+} hbtu_stats;
+
+/* Turn per-phase device timing on (1) or off (0; the default).  With timing
+ * off only total_ms and the counters are kept. */
+hbtu_status hbtu_set_timing(hbtu_handle *h, int32_t on);
+hbtu_status hbtu_get_stats(const hbtu_handle *h, hbtu_stats *out);
+hbtu_status hbtu_reset_stats(hbtu_handle *h);
+
+/* Message of the last failed call on this handle (or of the last failed
+ * hbtu_create when h is NULL). */
+const char *hbtu_last_error(const hbtu_handle *h);
+
+/* Library version, as major*10000 + minor*100 + patch. */
+int32_t hbtu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HBTU_H */

@@ -1,0 +1,116 @@
+"""Generate the golden fixtures of the unbinding path from the reference itself.
+
+Run here, where the reference sources are available:
+    python tests/golden/make_golden.py
+It builds oracle/_ref/libhbt_ref.so (the reference's own Subhalo_t::Unbind,
+compiled from its unmodified sources by oracle/Makefile) and writes one
+compressed .npz per case into tests/golden/.  Each file holds the inputs
+(particles in the order Unbind receives them, frame, parameters) and the
+reference's outputs (permuted particle order as input indices, Energies,
+Nbound, Mbound, frames, kinematics, per-type counts); `first_pass_*` cases hold
+the reference tree's BindingEnergy/EvaluatePotential of every particle.
+
+For sampled cases the stored particles are the ones AFTER the reference's
+random_shuffle (what the GPU library and the C oracle take), with
+mostbound_id naming the particle that was at position 0 before it.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from hbtplus_gb300 import synthetic as S  # noqa: E402
+from oracle import Oracle  # noqa: E402
+
+RESULT_KEYS = ("nbound", "mbound", "ref_pos", "ref_vel", "mostbound_pos", "mostbound_vel",
+               "specific_potential", "specific_kinetic", "specific_angmom", "nbound_type",
+               "mbound_type", "disrupted", "converged", "too_few")
+
+
+def scaled(n, seed, c=10.0, cf=0.1, center=None, bulk=(0.0, 0.0, 0.0)):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    r200 = 0.2 * (n / 1e5) ** (1.0 / 3.0)
+    sub = S.nfw_subhalo(rng, n, r200, c, contaminant_frac=cf, center=center,
+                        bulk_velocity=bulk)
+    S._assign_ids(rng, [sub])
+    return sub
+
+
+def save(name, params, sub, ref, shuffle_seed=0, drand_seed=1):
+    order, energy, res = ref.unbind(params, sub, nthreads=1, shuffle_seed=shuffle_seed,
+                                    drand_seed=drand_seed)
+    out = dict(sub)
+    if params["max_sample_size"] > 0 and len(sub["mass"]) > params["max_sample_size"]:
+        # store the post-shuffle particles, as the library takes them
+        perm = ref.reference_shuffle(len(sub["mass"]), shuffle_seed)
+        inv = np.empty_like(perm)
+        inv[perm] = np.arange(len(perm))
+        for k in ("id", "pos", "vel", "mass", "type"):
+            out[k] = sub[k][perm]
+        out["mostbound_id"] = int(sub["id"][0])
+        order = inv[order]
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"),
+        **{f"in_{k}": np.asarray(v) for k, v in out.items()},
+        **{f"par_{k}": np.asarray(v) for k, v in params.items()},
+        ref_order=order, ref_energy=energy, drand_seed=drand_seed,
+        **{f"ref_{k}": np.asarray(res[k]) for k in RESULT_KEYS})
+    print(f"{name}: n={len(sub['mass'])} nbound={res['nbound']} disrupted={res['disrupted']}")
+
+
+def save_first_pass(name, params, sub, ref):
+    E, pot, _ = ref.binding_energies(params, sub["pos"], sub["vel"], sub["mass"], sub["ref_pos"],
+                                     sub["ref_vel"], nthreads=1)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                        **{f"in_{k}": np.asarray(v) for k, v in sub.items()},
+                        **{f"par_{k}": np.asarray(v) for k, v in params.items()},
+                        ref_energy=E, ref_potential=pot)
+    print(f"{name}: n={len(sub['mass'])}")
+
+
+def main():
+    ref = Oracle(reference=True)
+    p = S.default_params()
+    save("nfw_1100", p, scaled(1000, 101), ref)
+    save("nfw_3300_corner", p, scaled(3000, 102, c=15.0, center=(0.01, 99.99, 50.0)), ref)
+    save("nfw_2200_bulk", p, scaled(2000, 103, c=6.0, bulk=(250.0, -120.0, 40.0)), ref)
+    save("nfw_1650_theta07", S.default_params(open_angle=0.7), scaled(1500, 104), ref)
+    save("nfw_1100_nonperiodic", S.default_params(periodic=0),
+         scaled(1000, 105, center=(40.0, 50.0, 60.0)), ref)
+    save("nfw_4400_sampled", S.default_params(max_sample_size=800),
+         scaled(4000, 106), ref, shuffle_seed=4242)
+    # a subhalo whose particles all move far too fast: disruption
+    hot = scaled(200, 107)
+    hot["vel"] = (hot["vel"] * 40.0).astype(np.float32)
+    save("disrupt_220", p, hot, ref)
+    save("tiny_5", p, scaled(5, 108, cf=0.0), ref)
+    two = scaled(2, 109, cf=0.0)
+    save("two_2", S.default_params(min_num_part=1), two, ref)
+    save("one_1", p, scaled(1, 110, cf=0.0), ref)
+    # coincident pairs below TreeNodeResolution: the reference's drand48 branch
+    co = scaled(800, 111)
+    co["pos"][1::7] = co["pos"][0::7][: len(co["pos"][1::7])]
+    save("coincident_880", p, co, ref, drand_seed=77)
+    save_first_pass("first_pass_nfw_3300", p, scaled(3000, 112), ref)
+    save_first_pass("first_pass_corner_2200", p, scaled(2000, 113, center=(99.995, 0.002, 0.5)),
+                    ref)
+    # a small batch: the halo-parallel loop of RefineParticles
+    b = S.subhalo_batch(nsub=48, seed=114, nmax=3000)
+    order, energy, res = ref.unbind_batch(p, b, nthreads=1)
+    np.savez_compressed(os.path.join(HERE, "batch_48.npz"),
+                        **{f"in_{k}": np.asarray(v) for k, v in b.items()},
+                        **{f"par_{k}": np.asarray(v) for k, v in p.items()},
+                        ref_order=order, ref_energy=energy,
+                        **{f"ref_{k}": np.array([r[k] for r in res]) for k in RESULT_KEYS})
+    print(f"batch_48: n={b['offsets'][-1]}")
+
+
+if __name__ == "__main__":
+    main()

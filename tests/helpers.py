@@ -1,0 +1,83 @@
+"""Shared helpers of the test suite: fixtures and comparisons."""
+from __future__ import annotations
+
+import glob
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+SINGLE_CASES = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                      if not os.path.basename(f).startswith(("first_pass", "batch")))
+FIRST_PASS_CASES = sorted(os.path.basename(f)[:-4]
+                          for f in glob.glob(os.path.join(GOLDEN, "first_pass_*.npz")))
+
+
+def load_case(name: str):
+    """(params, inputs, reference outputs) of a golden fixture."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    par = {k[4:]: z[k].item() for k in z.files if k.startswith("par_")}
+    inp = {k[3:]: z[k] for k in z.files if k.startswith("in_")}
+    for k in ("mostbound_id",):
+        if k in inp and inp[k].ndim == 0:
+            inp[k] = int(inp[k])
+    ref = {k[4:]: z[k] for k in z.files if k.startswith("ref_")}
+    extra = {k: z[k] for k in z.files if not k.startswith(("par_", "in_", "ref_"))}
+    ref.update(extra)
+    return par, inp, ref
+
+
+def tie_groups_equal(order_a, order_b, energy):
+    """Orders agree up to permutations inside runs of bit-equal energy."""
+    order_a = np.asarray(order_a)
+    order_b = np.asarray(order_b)
+    if len(order_a) != len(order_b):
+        return False
+    if np.array_equal(order_a, order_b):
+        return True
+    e = np.asarray(energy)
+    i = 0
+    n = len(e)
+    while i < n:
+        j = i + 1
+        while j < n and e[j] == e[i]:
+            j += 1
+        if set(order_a[i:j].tolist()) != set(order_b[i:j].tolist()):
+            return False
+        i = j
+    return True
+
+
+def partition_emulation(E: np.ndarray):
+    """The GPU's closed form of PartitionBindingEnergy (prefix counts of the
+    sign pattern), in numpy: returns (nbound, permutation of positions)."""
+    E = np.asarray(E, np.float32)
+    n = len(E)
+    if n == 0:
+        return 0, np.zeros(0, np.int64)
+    if n == 1:
+        return int(E[0] < 0), np.zeros(1, np.int64)
+    pos = np.nonzero(E[1:] > 0)[0] + 1          # P_1 < P_2 < ...
+    neg = np.nonzero(E[1:] < 0)[0][::-1] + 1    # Q_1 > Q_2 > ...
+    npos, nneg = len(pos), len(neg)
+    mn = min(npos, nneg)
+    k = np.arange(1, mn + 1)
+    failF = np.nonzero(pos[:mn] >= neg[:mn])[0]
+    F = (failF[0] + 1 if len(failF) else mn + 1) - 1
+    condG = np.array([(kk + 1 > nneg) or (pos[kk - 1] >= neg[kk]) for kk in k], bool)
+    failG = np.nonzero(condG)[0]
+    G = min((failG[0] + 1 if len(failG) else 1 << 30) - 1, F)
+    src = np.arange(n)
+    if nneg == 0:
+        mb = mf = vd = 0
+    else:
+        mb = 1 + G
+        mf = G + (1 if G + 1 <= F else 0)
+        vd = pos[mf - 1] if mf == mb else neg[mb - 1]
+        src[0] = neg[0]
+        for kk in range(1, mf + 1):
+            src[neg[kk - 1]] = pos[kk - 1]
+        for kk in range(1, mb):
+            src[pos[kk - 1]] = neg[kk]
+    src[vd] = 0
+    return int(vd + (E[0] < 0)), src

@@ -1,0 +1,250 @@
+"""GPU parity: the CUDA library through the C ABI against the reference.
+
+Ground truth is the reference's own Subhalo_t::Unbind (golden fixtures in
+tests/golden, generated by tests/golden/make_golden.py from the reference
+build) and the C oracle (oracle/hbt_oracle.c, pinned to the same fixtures by
+tests/test_oracle.py) for random inputs.
+
+Tolerances:
+  FP64 mode (HBTU_PRECISION_FP64): bit-exact -- same bound set, energies,
+    Nbound, Mbound, frames, order (up to runs of bit-equal energy, which the
+    reference's unstable std::sort may order either way); MboundType within
+    1e-4 relative (the reference's float accumulation); kinematics within 1e-6.
+  FP32 mode (default): a particle may change side only if its reference
+    energy lies inside the band |E| <= 1e-5 * max|E_bound|; Mbound within
+    1e-5 relative (+ one particle mass); energies within 2e-6 * max|E_bound|;
+    frames within 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+from helpers import FIRST_PASS_CASES, SINGLE_CASES, load_case, tie_groups_equal
+
+pytestmark = pytest.mark.gpu
+
+BAND = 1e-5
+EREL = 2e-6
+
+
+@pytest.fixture(scope="module")
+def U():
+    from hbtplus_gb300 import unbind
+    return unbind
+
+
+@pytest.fixture(scope="module")
+def orc():
+    from oracle import Oracle
+    return Oracle()
+
+
+def _bound_set(order, nb):
+    return set(np.asarray(order[:nb]).tolist())
+
+
+def check_exact(res, order, energy, ref, case, n):
+    nb = int(ref["nbound"])
+    assert res["nbound"] == nb, case
+    for k in ("mbound", "ref_pos", "ref_vel", "mostbound_pos", "mostbound_vel", "nbound_type",
+              "disrupted", "converged", "too_few"):
+        np.testing.assert_array_equal(np.asarray(res[k]), ref[k], err_msg=f"{case}: {k}")
+    # MboundType: the reference accumulates it in float (per OpenMP thread when
+    # Nbound > 100, src/subhalo.cpp:408-429), so its last bits follow the thread
+    # count; the library sums in double and rounds once.
+    np.testing.assert_allclose(np.asarray(res["mbound_type"]), ref["mbound_type"], rtol=1e-4,
+                               err_msg=f"{case}: mbound_type")
+    if n > 1:
+        for k in ("specific_potential", "specific_kinetic", "specific_angmom"):
+            np.testing.assert_allclose(np.asarray(res[k]), ref[k], rtol=1e-6, atol=1e-6,
+                                       err_msg=f"{case}: {k}")
+    np.testing.assert_array_equal(energy[:nb], ref["energy"][:nb])
+    if res["converged"]:
+        assert tie_groups_equal(order, ref["order"], energy), case
+    else:
+        np.testing.assert_array_equal(order, ref["order"])
+
+
+def check_band(res, order, energy, ref_order, ref_energy, ref_nb, ref_mbound, mass, case):
+    nb = res["nbound"]
+    emax = float(np.max(np.abs(ref_energy[:ref_nb]))) if ref_nb else 1.0
+    e_of = dict(zip(np.asarray(ref_order[:ref_nb]).tolist(),
+                    np.asarray(ref_energy[:ref_nb]).tolist()))
+    e_gpu = dict(zip(np.asarray(order).tolist(), np.asarray(energy).tolist()))
+    diff = _bound_set(order, nb) ^ _bound_set(ref_order, ref_nb)
+    outside = [k for k in diff if abs(e_of.get(k, e_gpu.get(k, 0.0))) > BAND * emax]
+    assert not outside, f"{case}: {len(outside)} particles changed side outside the band"
+    assert abs(res["mbound"] - ref_mbound) <= 1e-5 * ref_mbound + float(np.max(mass)) * len(diff) \
+        + 1e-12, case
+    common = min(nb, ref_nb)
+    if common and not diff:
+        ref_by_id = np.array([e_of[k] for k in np.asarray(order[:common]).tolist()])
+        assert np.max(np.abs(energy[:common] - ref_by_id)) <= EREL * emax, case
+    return len(diff)
+
+
+@pytest.mark.parametrize("case", SINGLE_CASES)
+def test_fp64_bit_exact_against_reference(U, case):
+    par, inp, ref = load_case(case)
+    with U.Unbinder(par, precision=1) as ub:
+        order, energy, res = ub.unbind(inp)
+    check_exact(res, order, energy, ref, case, len(inp["mass"]))
+
+
+@pytest.mark.parametrize("case", SINGLE_CASES)
+def test_fp32_within_band_of_reference(U, orc, case):
+    par, inp, ref = load_case(case)
+    with U.Unbinder(par, precision=0) as ub:
+        order, energy, res = ub.unbind(inp)
+    check_band(res, order, energy, ref["order"], ref["energy"], int(ref["nbound"]),
+               float(ref["mbound"]), inp["mass"], case)
+    assert res["disrupted"] == int(ref["disrupted"])
+    if len(inp["mass"]) > 1 and not res["disrupted"]:
+        np.testing.assert_allclose(res["ref_pos"], ref["ref_pos"], rtol=1e-6)
+        np.testing.assert_allclose(res["ref_vel"], ref["ref_vel"], rtol=1e-5, atol=1e-4)
+    _, _, ores = orc.unbind(par, inp, nthreads=1, drand_seed=int(ref["drand_seed"]))
+    assert res["iterations"] == ores["iterations"], case
+    assert res["interactions"] == ores["interactions"], case
+
+
+@pytest.mark.parametrize("case", FIRST_PASS_CASES)
+def test_first_pass_energies(U, case):
+    par, inp, ref = load_case(case)
+    with U.Unbinder(par, precision=1) as ub:
+        E, pot = ub.binding_energies(inp["pos"], inp["vel"], inp["mass"], inp["ref_pos"],
+                                     inp["ref_vel"])
+    np.testing.assert_array_equal(pot, ref["potential"])
+    np.testing.assert_array_equal(E, ref["energy"])
+    with U.Unbinder(par, precision=0) as ub:
+        E, pot = ub.binding_energies(inp["pos"], inp["vel"], inp["mass"], inp["ref_pos"],
+                                     inp["ref_vel"])
+    scale = np.maximum(np.abs(ref["potential"]), np.abs(ref["energy"]))
+    assert np.max(np.abs(pot - ref["potential"]) / np.abs(ref["potential"])) < 1e-6
+    assert np.max(np.abs(E - ref["energy"]) / scale) < 2e-6
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_batch_against_reference(U, precision):
+    par, inp, ref = load_case("batch_48")
+    with U.Unbinder(par, precision=precision) as ub:
+        order, energy, res = ub.unbind_batch(inp)
+    off = inp["offsets"]
+    for s in range(len(off) - 1):
+        a, b = off[s], off[s + 1]
+        if precision == 1:
+            r = {k: ref[k][s] for k in ("nbound", "mbound", "ref_pos", "ref_vel", "mostbound_pos",
+                                        "mostbound_vel", "nbound_type", "mbound_type",
+                                        "disrupted", "converged", "too_few",
+                                        "specific_potential", "specific_kinetic",
+                                        "specific_angmom")}
+            r["energy"] = ref["energy"][a:b]
+            r["order"] = ref["order"][a:b]
+            check_exact(res[s], order[a:b], energy[a:b], r, f"batch sub {s}", b - a)
+        else:
+            check_band(res[s], order[a:b], energy[a:b], ref["order"][a:b], ref["energy"][a:b],
+                       int(ref["nbound"][s]), float(ref["mbound"][s]), inp["mass"][a:b],
+                       f"batch sub {s}")
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_fp64_matches_oracle_random(U, orc, seed):
+    from hbtplus_gb300 import synthetic as S
+    rng = np.random.Generator(np.random.PCG64(700 + seed))
+    n = int(rng.integers(100, 6000))
+    center = rng.uniform(0, 100, 3)
+    if seed % 2:
+        center[rng.integers(3)] = rng.uniform(-0.01, 0.01) % 100.0
+    sub = S.nfw_subhalo(rng, n, 0.2 * (n / 1e5) ** (1 / 3), rng.uniform(5, 20),
+                        contaminant_frac=float(rng.uniform(0, 0.3)), center=center,
+                        bulk_velocity=rng.normal(0, 200, 3))
+    S._assign_ids(rng, [sub])
+    p = S.default_params(open_angle=float(rng.choice([0.3, 0.45, 0.7])),
+                         periodic=int(seed != 2))
+    o_ref, e_ref, r_ref = orc.unbind(p, sub, nthreads=4)
+    with U.Unbinder(p, precision=1) as ub:
+        order, energy, res = ub.unbind(sub)
+    nb = r_ref["nbound"]
+    assert res["nbound"] == nb
+    assert res["iterations"] == r_ref["iterations"]
+    assert res["interactions"] == r_ref["interactions"]
+    np.testing.assert_array_equal(energy[:nb], e_ref[:nb])
+    assert tie_groups_equal(order, o_ref, energy)
+    assert res["mbound"] == r_ref["mbound"]
+
+
+def test_single_subhalo_full_size(U, orc):
+    """The 1e5-particle NFW subhalo (+10% contaminants): FP32 against the oracle."""
+    from hbtplus_gb300 import synthetic as S
+    sub = S.single_subhalo(n=100_000)
+    p = S.default_params()
+    o_ref, e_ref, r_ref = orc.unbind(p, sub, nthreads=0)
+    with U.Unbinder(p, precision=0) as ub:
+        order, energy, res = ub.unbind(sub)
+    ndiff = check_band(res, order, energy, o_ref, e_ref, r_ref["nbound"], r_ref["mbound"],
+                       sub["mass"], "single_subhalo")
+    assert ndiff <= 2
+    assert res["iterations"] == r_ref["iterations"]
+    # size-independent properties: a permutation, energies sorted over the bound block
+    assert np.array_equal(np.sort(order), np.arange(len(order)))
+    nb = res["nbound"]
+    assert np.all(np.diff(energy[:nb]) >= 0) and np.all(energy[:nb] < 0)
+    assert abs(res["mbound"] - float(np.sum(sub["mass"][order[:nb]], dtype=np.float64))) < 1e-5
+
+
+def test_device_resident_call_matches_host_call(U):
+    torch = pytest.importorskip("torch")
+    from hbtplus_gb300 import synthetic as S
+    from hbtplus_gb300 import _lib
+    b = S.subhalo_batch(nsub=30, seed=5, nmax=4000)
+    p = S.default_params()
+    with U.Unbinder(p) as ub:
+        o_h, e_h, r_h = ub.unbind_batch(b)
+        dev = {k: torch.from_numpy(np.ascontiguousarray(b[k])).cuda()
+               for k in ("id", "pos", "vel", "mass", "type")}
+        n = int(b["offsets"][-1])
+        nsub = len(b["offsets"]) - 1
+        out = dict(order=torch.empty(n, dtype=torch.int64, device="cuda"),
+                   energy=torch.empty(n, dtype=torch.float32, device="cuda"),
+                   res=torch.empty(nsub * 192, dtype=torch.uint8, device="cuda"))
+        ub.unbind_batch_device(dev, b["offsets"], ub.make_states(b), out)
+        torch.cuda.synchronize()
+    assert np.array_equal(out["order"].cpu().numpy(), o_h)
+    assert np.array_equal(out["energy"].cpu().numpy(), e_h)
+    r_d = U.results_from_bytes(out["res"].cpu().numpy().tobytes(), nsub)
+    assert [r["nbound"] for r in r_d] == [r["nbound"] for r in r_h]
+    assert _lib.load().hbtu_version() >= 10000
+
+
+def test_edge_cases_and_errors(U):
+    from hbtplus_gb300 import _lib
+    from hbtplus_gb300 import synthetic as S
+    p = S.default_params()
+    rng = np.random.Generator(np.random.PCG64(9))
+    subs = [S.nfw_subhalo(rng, n, 0.01, 10.0, contaminant_frac=0.0) for n in (0, 1, 2, 3, 25)]
+    S._assign_ids(rng, subs)
+    b = S.concat(subs)
+    with U.Unbinder(p) as ub:
+        order, energy, res = ub.unbind_batch(b)
+        assert [r["nbound"] for r in res][:2] == [0, 1]
+        assert res[0]["too_few"] and res[1]["too_few"]
+        assert res[2]["disrupted"] and res[3]["disrupted"]  # fewer than MinNumPartOfSub
+        with pytest.raises(_lib.HBTUError) as ei:
+            bad = dict(b)
+            bad["offsets"] = np.array([0, 5, 3], np.int64)
+            ub.unbind_batch(bad)
+        assert ei.value.status == _lib.HBTU_ERR_INVALID_ARGUMENT
+    with pytest.raises(_lib.HBTUError) as ei:
+        U.Unbinder(S.default_params(softening=-1.0))
+    assert ei.value.status == _lib.HBTU_ERR_INVALID_ARGUMENT
+
+
+def test_pass_limit_reports_not_converged(U):
+    """A pass cap of 1 ends every multi-pass subhalo with HBTU_ERR_NOT_CONVERGED."""
+    from hbtplus_gb300 import _lib
+    from hbtplus_gb300 import synthetic as S
+    par, inp, ref = load_case("nfw_1100")
+    with U.Unbinder(par, max_passes=1) as ub:
+        with pytest.raises(_lib.HBTUError) as ei:
+            ub.unbind(inp)
+        assert ei.value.status == _lib.HBTU_ERR_NOT_CONVERGED
+        _, _, res = ub.unbind_batch(S.concat([inp]), check_status=False)
+        assert res[0]["status"] == _lib.HBTU_ERR_NOT_CONVERGED and res[0]["iterations"] == 1
