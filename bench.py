@@ -55,6 +55,8 @@ def parse():
                     help="batch: the 2000-subhalo batch (default); single: the isolated "
                          "1e5-particle NFW subhalo (+10%% contaminants)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--leaf-runs", type=int, default=-1,
+                    help="walk_leaf_runs option of the FP32 walk (-1: library default)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -204,7 +206,8 @@ def config_of(args, batch):
             "nsub": nsub, "particles": int(batch["offsets"][-1]),
             "max_subhalo": int(np.max(np.diff(batch["offsets"]))),
             "softening": 0.002, "open_angle": 0.45, "max_sample_size": 0,
-            "precision": args.precision, "l2": "flushed before each timed step (256 MB write)"}
+            "precision": args.precision, "walk_leaf_runs": args.leaf_runs if args.leaf_runs >= 0 else 1,
+            "l2": "flushed before each timed step (256 MB write)"}
 
 
 def main():
@@ -231,6 +234,8 @@ def main():
     ntot = int(batch["offsets"][-1])
     prec = 1 if args.precision == "fp64" else 0
     ub = U.Unbinder(params, precision=prec, device=local)
+    if args.leaf_runs >= 0:
+        ub.set_option("walk_leaf_runs", args.leaf_runs)
     stream = torch.cuda.current_stream(dev)
     ub.set_stream(stream.cuda_stream)
 

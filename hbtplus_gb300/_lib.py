@@ -91,6 +91,8 @@ SIGNATURES = {
                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "hbtu_last_error": (C.c_char_p, [C.c_void_p]),
     "hbtu_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
+    "hbtu_set_option": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
+    "hbtu_get_option": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int64)]),
     "hbtu_get_stats": (C.c_int, [C.c_void_p, C.POINTER(hbtu_stats)]),
     "hbtu_reset_stats": (C.c_int, [C.c_void_p]),
     "hbtu_version": (C.c_int32, []),

@@ -28,6 +28,8 @@ struct hbtu_handle {
   // tracing
   hbtu_stats stats{};
   bool timing = false;
+  // tuning options (hbtu_set_option)
+  int64_t opt_leaf_runs = 1;
   std::vector<cudaEvent_t> events;  // pool: 4 per pass when timing, 2 per call
 };
 
@@ -79,6 +81,7 @@ void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
   c.seg = cv.take<SegState>(S);
   c.plan = cv.take<PassPlan>(1);
   c.seg_off = cv.take<int>(S + 1);
+  c.seg_order = cv.take<int>(S);
   c.tree_base = cv.take<int>(S + 1);
   c.tgt_base = cv.take<int>(S + 1);
   c.tchunk_base = cv.take<int>(S + 1);
@@ -114,10 +117,10 @@ void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
   c.pending0 = cv.take<int>(N);
   c.mask = cv.take<unsigned long long>(N);
   c.X = cv.take<long long>(N + 1);
-  c.nd_abs = cv.take<float4>(2 * N);
-  c.nd_rel = cv.take<float4>(2 * N);
-  c.nd_len2 = cv.take<float>(2 * N);
-  c.nd_skip = cv.take<int>(2 * N);
+  // one spare slot: the walk prefetches node cur+1 speculatively
+  c.nd_abs = cv.take<float4>(2 * N + 1);
+  c.nd_rel = cv.take<float4>(2 * N + 1);
+  c.nd_meta = cv.take<int2>(2 * N + 1);
   c.pcode = cv.take<long long>(N + 1);
   c.pX = cv.take<long long>(N + 1);
   c.Pk = cv.take<int>(N);
@@ -251,14 +254,20 @@ hbtu_status setup_call(hbtu_handle *h, const hbtu_particles *p, long long S, con
     id = sg.id;
   }
   c.id = (long long *)id;
+  c.opt_leaf_runs = (int)h->opt_leaf_runs;
   std::vector<SegState> segs;
-  std::vector<int> segoff;
+  std::vector<int> segoff, order(S);
   init_states(h, S, offsets, st, segs, segoff);
+  for (long long s = 0; s < S; s++) order[s] = (int)s;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return segs[a].n > segs[b].n; });
   if (S > 0) {
     HBTU_CUDA(cudaMemcpyAsync(c.seg, segs.data(), sizeof(SegState) * S, cudaMemcpyHostToDevice,
                               c.st));
     HBTU_CUDA(cudaMemcpyAsync(c.seg_off, segoff.data(), sizeof(int) * (S + 1),
                               cudaMemcpyHostToDevice, c.st));
+    HBTU_CUDA(cudaMemcpyAsync(c.seg_order, order.data(), sizeof(int) * S, cudaMemcpyHostToDevice,
+                              c.st));
     // the staging copies above read host memory that lives until the call returns
   }
   if (N > 0) launch_init(c, pos, vel, mass, id);
@@ -466,6 +475,29 @@ hbtu_status hbtu_destroy(hbtu_handle *h)
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return HBTU_OK;
+}
+
+hbtu_status hbtu_set_option(hbtu_handle *h, const char *name, int64_t value)
+{
+  if (!h || !name) return HBTU_ERR_INVALID_ARGUMENT;
+  const std::string n(name);
+  if (n == "walk_leaf_runs") {
+    if (value != 0 && value != 1) return fail(h, HBTU_ERR_INVALID_ARGUMENT, "walk_leaf_runs: 0 or 1");
+    h->opt_leaf_runs = value;
+    return HBTU_OK;
+  }
+  return fail(h, HBTU_ERR_INVALID_ARGUMENT, "unknown option " + n);
+}
+
+hbtu_status hbtu_get_option(const hbtu_handle *h, const char *name, int64_t *value)
+{
+  if (!h || !name || !value) return HBTU_ERR_INVALID_ARGUMENT;
+  const std::string n(name);
+  if (n == "walk_leaf_runs") {
+    *value = h->opt_leaf_runs;
+    return HBTU_OK;
+  }
+  return HBTU_ERR_INVALID_ARGUMENT;
 }
 
 hbtu_status hbtu_set_timing(hbtu_handle *h, int32_t on)

@@ -98,6 +98,8 @@ struct Ctx {
   int *tree_base, *tgt_base;                 // S+1 each
   int *tchunk_base, *bchunk_base, *ub_base;  // S+1 each
   int *seg_off;                              // S+1
+  int *seg_order;                            // S: subhaloes by size, largest first
+  int opt_leaf_runs;                         // FP32 walk streams all-particle cells
   int *part_info;                            // 8 ints per segment
   unsigned *chunk_bbox;                      // 6 per chunk
   double *chunk_sums;                        // 16 per chunk
@@ -110,8 +112,7 @@ struct Ctx {
   long long *X;
   // nodes (2 per tree particle)
   float4 *nd_abs, *nd_rel;
-  float *nd_len2;
-  int *nd_skip;
+  int2 *nd_meta;  // {len*len as float bits (0 for particles), skip pointer}
   // partition
   long long *pcode, *pX;
   int *Pk, *Qk;

@@ -13,8 +13,9 @@
 //                       as the reference stores TreeCell_t::way.s)
 //               nd_rel  float4 {x, y, z, m} same, relative to the segment's
 //                       frame centre, wrapped once in double then cast
-//               nd_len2 float  len*len of the cell (0 for particle leaves)
-//               nd_skip int32  next node after this node's subtree
+//               nd_meta int2   {len*len of the cell as float bits (0 for
+//                       particle leaves; sign bit set on cells whose children
+//                       are all particles), next node after the subtree}
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

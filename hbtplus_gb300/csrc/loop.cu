@@ -128,6 +128,15 @@ __device__ int get_pass(const Ctx &c, int s, int *v)
   v[3] = sg.ub_hi - sg.ub_lo;
   return 0;
 }
+// targets of the pass, subhaloes in size order (largest first)
+__device__ int get_targets_sorted(const Ctx &c, int k, int *v)
+{
+  const SegState &sg = c.seg[c.seg_order[k]];
+  const bool act = sg.status == SEG_ACTIVE;
+  v[0] = act ? (sg.tgt_mode == 1 ? sg.coh_n : sg.ntgt) : 0;
+  v[1] = v[2] = v[3] = 0;
+  return 0;
+}
 __device__ int get_bound(const Ctx &c, int s, int *v)
 {
   const bool act = c.seg[s].status == SEG_ACTIVE;
@@ -165,15 +174,17 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode)
     int cnt = 0;
     for (int s = threadIdx.x; s < c.S; s += kPlanThreads) cnt += c.seg[s].status == SEG_ACTIVE;
     atomicAdd(&nact, cnt);
-    plan_scan4(c.S, get_pass, c, c.tree_base, c.tchunk_base, c.tgt_base, c.ub_base, tot);
+    plan_scan4(c.S, get_pass, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
     if (threadIdx.x == 0) {
       c.plan->nactive = nact;
       c.plan->ntree_total = tot[0];
       c.plan->nchunks_tree = tot[1];
-      c.plan->ntgt_total = tot[2];
       c.plan->nsort_total = tot[3];
       c.plan->max_levels = 0;
     }
+    __syncthreads();
+    plan_scan4(c.S, get_targets_sorted, c, c.tgt_base, nullptr, nullptr, nullptr, tot);
+    if (threadIdx.x == 0) c.plan->ntgt_total = tot[0];
   } else if (mode == 1) {
     plan_scan4(c.S, get_bound, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
     if (threadIdx.x == 0) c.plan->nchunks_bound = tot[0];

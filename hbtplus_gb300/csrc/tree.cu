@@ -249,12 +249,10 @@ __global__ void __launch_bounds__(kTB) k_leaves(Ctx c, int ntotal)
     const float4 r = make_rel(a, sg.fc, c.P);
     c.nd_abs[nb] = a;
     c.nd_rel[nb] = r;
-    c.nd_len2[nb] = fmul((float)sg.len, (float)sg.len);
-    c.nd_skip[nb] = nb + 2;
+    c.nd_meta[nb] = make_int2(__float_as_int(fmul((float)sg.len, (float)sg.len)), nb + 2);
     c.nd_abs[nb + 1] = a;
     c.nd_rel[nb + 1] = r;
-    c.nd_len2[nb + 1] = 0.f;
-    c.nd_skip[nb + 1] = nb + 2;
+    c.nd_meta[nb + 1] = make_int2(0, nb + 2);
     sg.nnodes = 2;
     return;
   }
@@ -262,8 +260,7 @@ __global__ void __launch_bounds__(kTB) k_leaves(Ctx c, int ntotal)
   const int idx = j + (int)(c.X[e + 1] - xb);
   c.nd_abs[nb + idx] = a;
   c.nd_rel[nb + idx] = make_rel(a, sg.fc, c.P);
-  c.nd_len2[nb + idx] = 0.f;
-  c.nd_skip[nb + idx] = nb + idx + 1;
+  c.nd_meta[nb + idx] = make_int2(0, nb + idx + 1);
   if (j == 0) sg.nnodes = n + (int)(c.X[base + n] - xb);
 }
 
@@ -287,8 +284,7 @@ __global__ void __launch_bounds__(kTB) k_cellnodes(Ctx c, int ntotal)
   for (int k = 0; k < od; k++)
     if (len >= (double)c.P.res) len = dmul(len, 0.5);
   const float lf = (float)len;
-  c.nd_len2[nb + idx] = fmul(lf, lf);
-  c.nd_skip[nb + idx] = nb + skip;
+  c.nd_meta[nb + idx] = make_int2(__float_as_int(fmul(lf, lf)), nb + skip);
   c.cidx[e] = nb + idx;
   c.cskip[e] = nb + skip;
   int p = c.parentI[e];
@@ -306,6 +302,11 @@ __global__ void __launch_bounds__(kTB) k_moments(Ctx c, int ntotal)
   if (e >= ntotal || !c.iscell[e] || c.pending0[e] != 0) return;
   const int s = c.sb.hi_a[e];
   const SegState &sg = c.seg[s];
+  {
+    // a cell without child cells: mark it for the walk's leaf runs (sign bit of len*len)
+    int2 *meta = &c.nd_meta[c.cidx[e]];
+    meta->x = meta->x | (int)0x80000000;
+  }
   for (int level = 0; level <= 2 * kMaxLevels + 2; level++) {
     const int idx = c.cidx[e], end = c.cskip[e];
     double m = 0., cx = 0., cy = 0., cz = 0.;
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(kTB) k_moments(Ctx c, int ntotal)
       cx = dadd(cx, dmul((double)a.x, w));
       cy = dadd(cy, dmul((double)a.y, w));
       cz = dadd(cz, dmul((double)a.z, w));
-      const int nk = c.nd_skip[k];
+      const int nk = c.nd_meta[k].y;
       k = nk > k ? nk : end;  // skip pointers always move forward
     }
     const float4 r = make_float4(__double2float_rn(ddiv(cx, m)), __double2float_rn(ddiv(cy, m)),

@@ -91,9 +91,10 @@ def nfw_subhalo(rng, n: int, r200: float, c: float, m: float = 1e-4,
         center = rng.uniform(0.0, box, size=3)
     center = np.asarray(center, np.float64)
     # previous most-bound particle: the one nearest the centre, moved to slot 0
-    k = int(np.argmin(np.einsum("ij,ij->i", pos, pos)))
     perm = np.arange(ntot)
-    perm[0], perm[k] = k, 0
+    if ntot:
+        k = int(np.argmin(np.einsum("ij,ij->i", pos, pos)))
+        perm[0], perm[k] = k, 0
     pos = pos[perm]
     vel = vel[perm]
     absolute = np.mod(pos + center, box)
@@ -106,7 +107,8 @@ def nfw_subhalo(rng, n: int, r200: float, c: float, m: float = 1e-4,
     return dict(pos=pos32, vel=vel32, mass=mass, type=typ,
                 ref_pos=center.astype(np.float32),
                 ref_vel=np.asarray(bulk_velocity, np.float32),
-                mostbound_pos=pos32[0].copy(), mostbound_vel=vel32[0].copy())
+                mostbound_pos=pos32[0].copy() if ntot else np.zeros(3, np.float32),
+                mostbound_vel=vel32[0].copy() if ntot else np.zeros(3, np.float32))
 
 
 def _assign_ids(rng, subs):

@@ -190,6 +190,14 @@ class Unbinder:
     def __exit__(self, *exc):
         self.close()
 
+    def set_option(self, name: str, value: int) -> None:
+        _lib.check(self.lib.hbtu_set_option(self.handle, name.encode(), int(value)), self.handle)
+
+    def get_option(self, name: str) -> int:
+        v = C.c_int64()
+        _lib.check(self.lib.hbtu_get_option(self.handle, name.encode(), C.byref(v)), self.handle)
+        return v.value
+
     def set_timing(self, on: bool) -> None:
         _lib.check(self.lib.hbtu_set_timing(self.handle, int(bool(on))), self.handle)
 

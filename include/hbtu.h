@@ -173,6 +173,12 @@ hbtu_status hbtu_set_timing(hbtu_handle *h, int32_t on);
 hbtu_status hbtu_get_stats(const hbtu_handle *h, hbtu_stats *out);
 hbtu_status hbtu_reset_stats(hbtu_handle *h);
 
+/* Tuning options of a handle (results do not depend on them):
+ *   "walk_leaf_runs"  1 (default) or 0: the FP32 walk streams the particles of
+ *                     a cell whose children are all particles. */
+hbtu_status hbtu_set_option(hbtu_handle *h, const char *name, int64_t value);
+hbtu_status hbtu_get_option(const hbtu_handle *h, const char *name, int64_t *value);
+
 /* Message of the last failed call on this handle (or of the last failed
  * hbtu_create when h is NULL). */
 const char *hbtu_last_error(const hbtu_handle *h);
