@@ -1,0 +1,84 @@
+// shim_lib.cpp -- test harness of include/hbtu_subhalo.hpp.
+//
+// Stand-ins for HBT+'s Particle_t / Subhalo_t / Snapshot_t with the member
+// names and types of src/snapshot.h:51-72 and src/subhalo.h:24-146 (HBT_INT8,
+// float HBTReal), so the shim is exercised exactly as the reference would use
+// it.  shim_unbind() builds one subhalo, calls hbtu::UnbindGPU and reports the
+// subhalo as Unbind leaves it.
+#include <array>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "hbtu_subhalo.hpp"
+
+namespace mock {
+typedef std::array<float, 3> HBTxyz;
+struct Particle_t {
+  long Id;
+  HBTxyz ComovingPosition;
+  HBTxyz PhysicalVelocity;
+  float Mass;
+  int Type;
+};
+struct Subhalo_t {
+  long TrackId = 0, Nbound = 0;
+  float Mbound = 0;
+  long NboundType[6] = {0};
+  float MboundType[6] = {0};
+  int SnapshotIndexOfDeath = -1, SnapshotIndexOfSink = -1;
+  float SpecificSelfPotentialEnergy = 0, SpecificSelfKineticEnergy = 0;
+  float SpecificAngularMomentum[3] = {0, 0, 0};
+  HBTxyz ComovingAveragePosition, PhysicalAverageVelocity, ComovingMostBoundPosition,
+      PhysicalMostBoundVelocity;
+  long SinkTrackId = -1;
+  std::vector<Particle_t> Particles;
+  bool IsTrapped() { return SinkTrackId != -1; }
+  bool IsAlive() { return SnapshotIndexOfDeath == -1; }
+};
+struct Snapshot_t {
+  int GetSnapshotIndex() const { return 7; }
+};
+}  // namespace mock
+
+extern "C" int shim_unbind(hbtu_handle *h, const hbtu_params *par, int64_t n, const int64_t *id,
+                           const float *pos, const float *vel, const float *mass,
+                           const int32_t *type, const hbtu_state *st, int64_t *out_id,
+                           float *out_energy, hbtu_result *out, int32_t *death)
+{
+  mock::Subhalo_t s;
+  s.Particles.resize(n);
+  for (int64_t i = 0; i < n; i++) {
+    s.Particles[i].Id = id[i];
+    for (int j = 0; j < 3; j++) {
+      s.Particles[i].ComovingPosition[j] = pos[3 * i + j];
+      s.Particles[i].PhysicalVelocity[j] = vel[3 * i + j];
+    }
+    s.Particles[i].Mass = mass[i];
+    s.Particles[i].Type = type ? type[i] : 1;
+  }
+  for (int j = 0; j < 3; j++) {
+    s.ComovingAveragePosition[j] = st->ref_pos[j];
+    s.PhysicalAverageVelocity[j] = st->ref_vel[j];
+    s.ComovingMostBoundPosition[j] = st->mostbound_pos[j];
+    s.PhysicalMostBoundVelocity[j] = st->mostbound_vel[j];
+  }
+  mock::Snapshot_t epoch;
+  std::vector<float> energies;
+  const hbtu_status rc = hbtu::UnbindGPU(h, *par, s, epoch, &energies);
+  if (rc != HBTU_OK) return rc;
+  for (int64_t i = 0; i < n; i++) out_id[i] = s.Particles[i].Id;
+  for (size_t i = 0; i < energies.size(); i++) out_energy[i] = energies[i];
+  std::memset(out, 0, sizeof(*out));
+  out->nbound = s.Nbound;
+  out->mbound = s.Mbound;
+  for (int j = 0; j < 3; j++) {
+    out->ref_pos[j] = s.ComovingAveragePosition[j];
+    out->ref_vel[j] = s.PhysicalAverageVelocity[j];
+    out->mostbound_pos[j] = s.ComovingMostBoundPosition[j];
+    out->mostbound_vel[j] = s.PhysicalMostBoundVelocity[j];
+  }
+  for (int t = 0; t < 6; t++) out->nbound_type[t] = s.NboundType[t];
+  *death = s.SnapshotIndexOfDeath;
+  return HBTU_OK;
+}

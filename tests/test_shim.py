@@ -1,0 +1,82 @@
+"""The C++ drop-in (include/hbtu_subhalo.hpp) used the way HBT+ would use it.
+
+CPU: the shim compiles against stand-ins with the reference's member names
+(tests/shim/shim_lib.cpp) and, where the reference sources are present,
+against the reference's own headers.  GPU: the compiled harness unbinds golden
+subhaloes through hbtu::UnbindGPU and leaves them as the reference's Unbind
+does (FP64 mode: bit-exact Nbound, Mbound, order and Energies)."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from helpers import load_case
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SHIM = os.path.join(ROOT, "tests", "shim")
+SO = os.path.join(SHIM, "_build", "libshim.so")
+REF_SRC = "/root/reference/src"
+
+
+def build_shim():
+    from hbtplus_gb300 import build as B
+    lib = B.build()
+    os.makedirs(os.path.dirname(SO), exist_ok=True)
+    subprocess.run(["g++", "-std=c++11", "-O2", "-fPIC", "-shared", "-I",
+                    os.path.join(ROOT, "include"), os.path.join(SHIM, "shim_lib.cpp"), lib,
+                    "-Wl,-rpath," + os.path.dirname(lib), "-o", SO], check=True)
+    return SO
+
+
+def test_shim_compiles():
+    assert os.path.exists(build_shim())
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+def test_shim_compiles_against_reference_types(tmp_path):
+    src = tmp_path / "use_ref.cpp"
+    src.write_text('#include "subhalo.h"\n#include "hbtu_subhalo.hpp"\n'
+                   "void f(hbtu_handle *h, const hbtu_params &p, Subhalo_t &s, const Snapshot_t &e)"
+                   "{ std::vector<float> E; hbtu::UnbindGPU(h, p, s, e, &E); "
+                   "std::vector<Subhalo_t> v(1); hbtu::UnbindBatchGPU(h, p, v, {0}, e); }\n")
+    subprocess.run(["g++", "-std=c++11", "-fsyntax-only", "-DHBT_INT8", "-w",
+                    "-I", os.path.join(ROOT, "oracle", "ref", "stubs"), "-I", REF_SRC,
+                    "-I", os.path.join(ROOT, "include"), str(src)], check=True)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["nfw_2200_bulk", "nfw_3300_corner", "disrupt_220"])
+def test_shim_unbind_matches_reference(case):
+    from hbtplus_gb300 import _lib
+    from hbtplus_gb300.unbind import Unbinder, _state, params_from_dict
+    so = C.CDLL(build_shim())
+    par, inp, ref = load_case(case)
+    n = len(inp["mass"])
+    cp = params_from_dict(par, precision=1)
+    st = _state(inp["ref_pos"], inp["ref_vel"], inp["mostbound_pos"], inp["mostbound_vel"],
+                inp["id"][0])
+    arr = {k: np.ascontiguousarray(inp[k]) for k in ("id", "pos", "vel", "mass", "type")}
+    out_id = np.zeros(n, np.int64)
+    out_e = np.zeros(n, np.float32)
+    res = _lib.hbtu_result()
+    death = C.c_int32(0)
+    with Unbinder(par, precision=1) as ub:
+        rc = so.shim_unbind(ub.handle, C.byref(cp), C.c_int64(n),
+                            *[C.c_void_p(arr[k].ctypes.data)
+                              for k in ("id", "pos", "vel", "mass", "type")],
+                            C.byref(st), C.c_void_p(out_id.ctypes.data),
+                            C.c_void_p(out_e.ctypes.data), C.byref(res), C.byref(death))
+    assert rc == 0
+    nb = int(ref["nbound"])
+    assert res.nbound == nb and res.mbound == float(ref["mbound"])
+    np.testing.assert_array_equal(np.array(list(res.ref_pos), np.float32), ref["ref_pos"])
+    ref_ids = inp["id"][ref["order"]]
+    if int(ref["disrupted"]):
+        np.testing.assert_array_equal(out_id, ref_ids)
+        assert death.value == 7  # SnapshotIndexOfDeath set by the disruption branch
+    else:
+        np.testing.assert_array_equal(out_e[:nb], ref["energy"][:nb])
+        assert set(out_id[:nb].tolist()) == set(ref_ids[:nb].tolist())
+        assert death.value == -1
