@@ -18,6 +18,8 @@ HBTU_ERR_NOT_CONVERGED = 4
 HBTU_ERR_NO_DEVICE = 5
 HBTU_ERR_TOO_LARGE = 6
 
+HBTU_NOALLOC_MAX_PARTICLES = 16384
+
 HBTU_PRECISION_FP32 = 0
 HBTU_PRECISION_FP64 = 1
 HBTU_HOST = 0
@@ -96,6 +98,9 @@ SIGNATURES = {
     "hbtu_get_stats": (C.c_int, [C.c_void_p, C.POINTER(hbtu_stats)]),
     "hbtu_reset_stats": (C.c_int, [C.c_void_p]),
     "hbtu_version": (C.c_int32, []),
+    "hbtu_unbind_noalloc": (C.c_int, [C.POINTER(hbtu_params), C.POINTER(hbtu_particles), C.c_int64,
+                                      C.POINTER(hbtu_state), C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p]),
 }
 
 _LIB = None

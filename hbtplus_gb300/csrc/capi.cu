@@ -9,12 +9,14 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstdarg>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
 #include <vector>
 
-#include "device_common.cuh"
+#include "driver.h"
 
 struct hbtu_handle {
   hbtu_params params;
@@ -34,11 +36,6 @@ struct hbtu_handle {
 };
 
 namespace hbtu {
-namespace {
-
-thread_local std::string g_create_error;
-
-int max_passes_of(const hbtu_params &p) { return p.max_passes > 0 ? p.max_passes : 10000; }
 
 // Carves the workspace; with base == nullptr it only measures.
 struct Carver {
@@ -55,17 +52,7 @@ struct Carver {
   }
 };
 
-struct Staging {
-  float *pos, *vel, *mass;
-  long long *id;
-  int *type;
-  long long *order;
-  float *energy;
-  double *pot;
-  hbtu_result *res;
-};
-
-void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
+static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
 {
   const long long maxchunks = N / kChunk + S + 2;
   c.pm = cv.take<float4>(N);
@@ -145,6 +132,29 @@ size_t workspace_bytes(long long N, long long S)
   return cv.off + 256;
 }
 
+void carve_workspace(char *base, Ctx &c, Staging &sg, long long N, long long S)
+{
+  Carver cv(base);
+  carve(cv, c, sg, N, S);
+}
+
+// Message of the last failed call made without a handle (fixed buffer: the
+// allocation-free entry point may write it).
+thread_local char g_error_buf[512];
+
+void set_global_error(const char *fmt, ...)
+{
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_error_buf, sizeof(g_error_buf), fmt, ap);
+  va_end(ap);
+}
+
+namespace {
+
+int max_passes_of(const hbtu_params &p) { return p.max_passes > 0 ? p.max_passes : 10000; }
+
+
 hbtu_status fail(hbtu_handle *h, hbtu_status st, const std::string &msg)
 {
   if (h) h->err = msg;
@@ -179,30 +189,8 @@ void init_states(const hbtu_handle *h, long long S, const int64_t *offsets, cons
   segs.assign(S, SegState());
   segoff.resize(S + 1);
   for (long long s = 0; s <= S; s++) segoff[s] = (int)offsets[s];
-  for (long long s = 0; s < S; s++) {
-    SegState g;
-    memset(&g, 0, sizeof(g));
-    g.off = (int)offsets[s];
-    g.n = (int)(offsets[s + 1] - offsets[s]);
-    g.status = g.n <= 1 ? SEG_TRIVIAL : SEG_ACTIVE;
-    g.nbound = g.nlast = g.n;
-    g.mode = MODE_FULL;
-    g.first_mb = INT_MAX;
-    const bool sampling = ms > 0 && g.n > ms;
-    g.t0 = 0;
-    g.ntree = sampling ? (int)ms : g.n;
-    g.mfac = sampling ? (float)g.n / (float)ms : 1.f;  // (HBTReal)Nlast/MaxSampleSize
-    g.ntgt = g.n;
-    g.tgt_mode = sampling ? 2 : 0;
-    for (int j = 0; j < 3; j++) {
-      g.ref_pos[j] = st[s].ref_pos[j];
-      g.ref_vel[j] = st[s].ref_vel[j];
-      g.mb_pos[j] = st[s].mostbound_pos[j];
-      g.mb_vel[j] = st[s].mostbound_vel[j];
-    }
-    g.mb_id = st[s].mostbound_id;
-    segs[s] = g;
-  }
+  for (long long s = 0; s < S; s++)
+    init_segment(segs[s], (int)offsets[s], (int)(offsets[s + 1] - offsets[s]), st[s], ms);
 }
 
 // Shared set-up of a call: checks, workspace, staging, segment states, init kernel.
@@ -228,8 +216,7 @@ hbtu_status setup_call(hbtu_handle *h, const hbtu_particles *p, long long S, con
   hbtu_status rc = ensure_workspace(h, N, S);
   if (rc != HBTU_OK) return rc;
   HBTU_CUDA(cudaSetDevice(h->device));
-  Carver cv(h->ws);
-  carve(cv, c, sg, N, S);
+  carve_workspace(h->ws, c, sg, N, S);
   c.P = h->dp;
   c.N = (int)N;
   c.S = (int)S;
@@ -275,12 +262,6 @@ hbtu_status setup_call(hbtu_handle *h, const hbtu_particles *p, long long S, con
   return HBTU_OK;
 }
 
-void read_plan(Ctx &c)
-{
-  HBTU_CUDA(cudaMemcpyAsync(c.plan_host, c.plan, sizeof(PassPlan), cudaMemcpyDeviceToHost, c.st));
-  HBTU_CUDA(cudaStreamSynchronize(c.st));
-}
-
 cudaEvent_t event_at(hbtu_handle *h, size_t k)
 {
   while (h->events.size() <= k) {
@@ -293,19 +274,20 @@ cudaEvent_t event_at(hbtu_handle *h, size_t k)
 
 // Phase timer: with timing on, events bracket tree / walk / loop kernels of
 // each pass; elapsed times are read once the stream has passed them.
-struct PhaseTimer {
+struct PhaseTimer : LoopHooks {
   hbtu_handle *h;
   cudaStream_t st;
   size_t next = 2;  // events 0, 1 bracket the whole call
   std::vector<size_t> marks;
-  void mark()
+  PhaseTimer(hbtu_handle *hh, cudaStream_t s) : h(hh), st(s) { stats = &hh->stats; }
+  void mark() override
   {
     if (!h->timing) return;
     HBTU_CUDA(cudaEventRecord(event_at(h, next), st));
     marks.push_back(next++);
   }
   // marks come in groups of 4: before tree, after tree, after walk, after loop
-  void collect()
+  void collect() override
   {
     for (size_t i = 0; i + 3 < marks.size(); i += 4) {
       float a = 0, b = 0, c = 0;
@@ -321,36 +303,76 @@ struct PhaseTimer {
   }
 };
 
-// One pass's tree and energies for every active subhalo.
-void pass_tree_and_energies(hbtu_handle *h, Ctx &c, PhaseTimer *pt)
-{
-  const PassPlan pl = *c.plan_host;
-  if (pt) pt->mark();
-  launch_tree_build(c, pl);
-  if (pt) pt->mark();
-  launch_walk(c, pl);
-  h->stats.walk_launches += pl.ntgt_total > 0;
-  if (pt) pt->mark();
-}
-
 hbtu_status run_loop(hbtu_handle *h, Ctx &c)
 {
-  const int maxp = max_passes_of(h->params);
+  PhaseTimer pt(h, c.st);
+  run_passes(c, max_passes_of(h->params), &pt);
+  return HBTU_OK;
+}
+
+}  // namespace
+
+void init_segment(SegState &g, int off, int n, const hbtu_state &st, long long maxsample)
+{
+  memset(&g, 0, sizeof(g));
+  g.off = off;
+  g.n = n;
+  g.status = n <= 1 ? SEG_TRIVIAL : SEG_ACTIVE;
+  g.nbound = g.nlast = n;
+  g.mode = MODE_FULL;
+  g.first_mb = INT_MAX;
+  const bool sampling = maxsample > 0 && n > maxsample;
+  g.t0 = 0;
+  g.ntree = sampling ? (int)maxsample : n;
+  g.mfac = sampling ? (float)n / (float)maxsample : 1.f;  // (HBTReal)Nlast/MaxSampleSize
+  g.ntgt = n;
+  g.tgt_mode = sampling ? 2 : 0;
+  for (int j = 0; j < 3; j++) {
+    g.ref_pos[j] = st.ref_pos[j];
+    g.ref_vel[j] = st.ref_vel[j];
+    g.mb_pos[j] = st.mostbound_pos[j];
+    g.mb_vel[j] = st.mostbound_vel[j];
+  }
+  g.mb_id = st.mostbound_id;
+}
+
+void read_plan(Ctx &c)
+{
+  HBTU_CUDA(cudaMemcpyAsync(c.plan_host, c.plan, sizeof(PassPlan), cudaMemcpyDeviceToHost, c.st));
+  HBTU_CUDA(cudaStreamSynchronize(c.st));
+}
+
+// One pass's tree and energies for every active subhalo.
+void pass_tree_and_energies(Ctx &c, LoopHooks *hk)
+{
+  const PassPlan pl = *c.plan_host;
+  if (hk) hk->mark();
+  launch_tree_build(c, pl);
+  if (hk) hk->mark();
+  launch_walk(c, pl);
+  if (hk && hk->stats) hk->stats->walk_launches += pl.ntgt_total > 0;
+  if (hk) hk->mark();
+}
+
+// The unbinding loop of all subhaloes of a call (src/subhalo_unbind.cpp:310-422),
+// then the final energy sort and RefineBindingEnergyOrder.  One host read of a
+// small plan per pass.
+void run_passes(Ctx &c, int max_passes, LoopHooks *hk)
+{
   const int max_chunks = c.N / kChunk + c.S + 1;
-  PhaseTimer pt{h, c.st};
   for (;;) {
     launch_plan(c, 0);
     launch_bbox_cube(c, max_chunks);
     read_plan(c);
-    pt.collect();
+    if (hk) hk->collect();
     const PassPlan pl = *c.plan_host;
     launch_block_sort(c, pl.nsort_total, 0);  // unbound blocks of the previous pass
     if (pl.nactive == 0) break;
-    h->stats.passes++;
-    pass_tree_and_energies(h, c, &pt);
+    if (hk && hk->stats) hk->stats->passes++;
+    pass_tree_and_energies(c, hk);
     launch_partition(c);
-    launch_averages_control(c, maxp);
-    pt.mark();
+    launch_averages_control(c, max_passes);
+    if (hk) hk->mark();
   }
   launch_plan(c, 2);
   read_plan(c);
@@ -359,19 +381,16 @@ hbtu_status run_loop(hbtu_handle *h, Ctx &c)
   if (nrefine > 0) {  // RefineBindingEnergyOrder (:406-407)
     launch_refine_mode(c, 1);
     launch_plan(c, 0);
-    launch_bbox_cube(c, c.N / kChunk + c.S + 1);
+    launch_bbox_cube(c, max_chunks);
     read_plan(c);
-    pass_tree_and_energies(h, c, nullptr);
+    pass_tree_and_energies(c, nullptr);
     launch_refine_mode(c, 0);
     launch_plan(c, 3);
     read_plan(c);
     launch_block_sort(c, c.plan_host->nsort_total, 2);
     launch_plan(c, 2);  // chunk plan of the kinematics
   }
-  return HBTU_OK;
 }
-
-}  // namespace
 
 DevParams derive_params(const hbtu_params &p)
 {
@@ -408,13 +427,13 @@ int32_t hbtu_version(void) { return 10000; }
 
 const char *hbtu_last_error(const hbtu_handle *h)
 {
-  return h ? h->err.c_str() : g_create_error.c_str();
+  return h ? h->err.c_str() : g_error_buf;
 }
 
 hbtu_status hbtu_create(const hbtu_params *params, hbtu_handle **out)
 {
   if (!params || !out) {
-    g_create_error = "null params or output pointer";
+    set_global_error("null params or output pointer");
     return HBTU_ERR_INVALID_ARGUMENT;
   }
   *out = nullptr;
@@ -423,29 +442,30 @@ hbtu_status hbtu_create(const hbtu_params *params, hbtu_handle **out)
       params->min_num_part < 0 || params->max_sample_size < 0 ||
       (params->periodic && !(params->box_size > 0)) || !(params->scale_factor > 0) ||
       (params->precision != HBTU_PRECISION_FP32 && params->precision != HBTU_PRECISION_FP64)) {
-    g_create_error =
+    set_global_error(
         "invalid parameters: need softening > 0, open_angle >= 0, 0 < bound_mass_precision <= 1, "
         "min_num_part >= 0, max_sample_size >= 0, box_size > 0 when periodic, scale_factor > 0, "
-        "precision FP32 or FP64";
+        "precision FP32 or FP64");
     return HBTU_ERR_INVALID_ARGUMENT;
   }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= params->device || params->device < 0) {
     cudaGetLastError();
-    g_create_error = "no CUDA device " + std::to_string(params->device);
+    set_global_error("no CUDA device %d", params->device);
     return HBTU_ERR_NO_DEVICE;
   }
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, params->device) != cudaSuccess || prop.major != 10 ||
       prop.minor != 3) {
     cudaGetLastError();
-    g_create_error = "device " + std::to_string(params->device) +
-                     " is not compute capability 10.3 (this library is built for sm_103a only)";
+    set_global_error("device %d is not compute capability 10.3 (this library is built for sm_103a "
+                     "only)",
+                     params->device);
     return HBTU_ERR_NO_DEVICE;
   }
   hbtu_handle *h = new (std::nothrow) hbtu_handle();
   if (!h) {
-    g_create_error = "out of host memory";
+    set_global_error("out of host memory");
     return HBTU_ERR_OUT_OF_MEMORY;
   }
   h->params = *params;
@@ -454,7 +474,7 @@ hbtu_status hbtu_create(const hbtu_params *params, hbtu_handle **out)
   if (cudaSetDevice(h->device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMallocHost(&h->plan_host, sizeof(PassPlan)) != cudaSuccess) {
-    g_create_error = std::string("CUDA set-up failed: ") + cudaGetErrorString(cudaGetLastError());
+    set_global_error("CUDA set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return HBTU_ERR_CUDA;
@@ -631,7 +651,7 @@ hbtu_status hbtu_binding_energies(hbtu_handle *h, const hbtu_particles *p, int64
     launch_plan(c, 0);
     launch_bbox_cube(c, c.N / kChunk + 2);
     read_plan(c);
-    pass_tree_and_energies(h, c, nullptr);
+    pass_tree_and_energies(c, nullptr);
     float *en = host ? sg.energy : energy_out;
     HBTU_CUDA(cudaMemcpyAsync(en, c.eE, sizeof(float) * n, cudaMemcpyDeviceToDevice, c.st));
     if (host) {

@@ -153,6 +153,30 @@ hbtu_status hbtu_binding_energies(hbtu_handle *h, const hbtu_particles *p, int64
                                   const float ref_pos[3], const float ref_vel[3],
                                   float *energy_out, double *potential_out);
 
+/* Largest subhalo hbtu_unbind_noalloc accepts (its fixed scratch capacity). */
+#define HBTU_NOALLOC_MAX_PARTICLES 16384
+
+/* hbtu_unbind for callers that cannot allocate GPU memory (code running
+ * inside another framework's memory pool, a process whose device memory is
+ * reserved up front, a pipeline that forbids allocation after start-up).  No
+ * counterpart in the reference: it is an addition of this library.
+ *   - no handle: params as for hbtu_create; runs on the current device and on
+ *     cuda_stream (NULL: the default stream);
+ *   - p, order_out, energy_out and res must all be device memory
+ *     (p->location == HBTU_DEVICE); st is host memory;
+ *   - working memory is a fixed 8 MiB array inside the library, held by every
+ *     GPU that loads it until exit; subhaloes of more than
+ *     HBTU_NOALLOC_MAX_PARTICLES particles return HBTU_ERR_TOO_LARGE;
+ *   - the first call on a device looks up the array's device address; make
+ *     that call before any stream capture;
+ *   - all calls share the array: calls that overlap on the GPU race, so
+ *     serialise them;
+ *   - it calls no cudaMalloc, cudaFree or other allocating routine.
+ * Errors are reported by hbtu_last_error(NULL). */
+hbtu_status hbtu_unbind_noalloc(const hbtu_params *params, const hbtu_particles *p, int64_t n,
+                                const hbtu_state *st, int64_t *order_out, float *energy_out,
+                                hbtu_result *res, void *cuda_stream);
+
 /* Counters and device timings accumulated by a handle (tracing). */
 typedef struct hbtu_stats {
   double total_ms;         /* device time of the unbinding calls, CUDA events on the handle's stream */
