@@ -42,6 +42,11 @@ UNIT = "subhalo unbinds/s"
 FLOPS_PER_INTERACTION = 14  # 3 sub, 5 for r^2, 4 for rsqrt, 2 for the potential update
 HBM_BYTES_PER_EVALUATION = 44  # read pos, vel, mass (28 B); write E and index (16 B)
 FP32_LANES_PER_SM = 128
+# DRAM bytes (read + write) of the first-pass walk launch, from one ncu capture of
+# the same workload (summaries in profiles/); None until captured for this kernel.
+WALK1_DRAM_BYTES = {"batch": 69318912, "single": 8256512}
+WALK1_PROFILE = {"batch": "walk_fp32_pass1_batch2000.md",
+                 "single": "walk_fp32_pass1_single1e5.md"}
 
 
 def parse():
@@ -290,29 +295,40 @@ def main():
     value = ws * nsub / (ms_per_step / 1e3)
     clocks = clk.summary()
 
-    # -- roofline of the dominant kernel (the energy walk) ----------------------
+    # -- roofline of the dominant kernel launch: the first pass's energy walk ----
     walk_ms = st["walk_ms"] / args.steps
+    walk1_ms = st["walk1_ms"] / args.steps
+    walk1_inter = st["walk1_interactions"] / args.steps
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     mhz = clocks.get("sm_mhz") or 1965.0
     fp32_peak = sm_count * FP32_LANES_PER_SM * 2 * mhz * 1e6 / 1e12
-    achieved = interactions * FLOPS_PER_INTERACTION / (walk_ms / 1e3) / 1e12 if walk_ms else 0.0
+    achieved = walk1_inter * FLOPS_PER_INTERACTION / (walk1_ms / 1e3) / 1e12 if walk1_ms else 0.0
+    achieved_all = interactions * FLOPS_PER_INTERACTION / (walk_ms / 1e3) / 1e12 if walk_ms else 0
     peaks, peak_kind = measured_peaks()
-    hbm_achieved = evaluations * HBM_BYTES_PER_EVALUATION / (walk_ms / 1e3) / 1e9 if walk_ms else 0
+    first_evals = ntot  # the first pass evaluates every particle once
+    hbm_achieved = (first_evals * HBM_BYTES_PER_EVALUATION / (walk1_ms / 1e3) / 1e9
+                    if walk1_ms else 0.0)
+    traffic = WALK1_DRAM_BYTES.get(args.workload) if args.precision == "fp32" else None
     roofline = {
-        "kernel": "k_walk (Barnes-Hut energy walk)",
+        "kernel": "k_walk_fp32, first pass of the step (Barnes-Hut energy walk)",
         "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
         "frac": achieved / fp32_peak if fp32_peak else None,
         "peak_source": f"{sm_count} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 flop at the "
                        f"measured median SM clock {mhz:.0f} MHz (FP32 FMA rate; no FP32 figure "
                        "in MEASURED_PEAKS.json)",
-        "traffic": None,
+        "traffic": traffic,
+        "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of this launch, "
+                           "profiles/" + WALK1_PROFILE[args.workload]) if traffic else None,
         "flops_per_interaction": FLOPS_PER_INTERACTION,
-        "interactions_per_step": interactions, "walk_ms_per_step": walk_ms,
-        "walk_share_of_step": walk_ms / ms_per_step if ms_per_step else None,
+        "interactions_per_launch": walk1_inter, "launch_ms": walk1_ms,
+        "all_walk_launches": {"achieved": achieved_all, "interactions_per_step": interactions,
+                              "walk_ms_per_step": walk_ms,
+                              "share_of_step": walk_ms / ms_per_step if ms_per_step else None},
         "hbm": {"bound": "hbm", "achieved": hbm_achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": hbm_achieved / peaks["hbm_gbs"],
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                "bytes_per_evaluation": HBM_BYTES_PER_EVALUATION},
+                "bytes_per_evaluation": HBM_BYTES_PER_EVALUATION,
+                "algorithmic_bytes_per_launch": first_evals * HBM_BYTES_PER_EVALUATION},
     }
 
     # -- e2e: host buffers through the C ABI, pinned memory -----------------------

@@ -76,6 +76,7 @@ class hbtu_stats(C.Structure):
         ("loop_ms", C.c_double), ("calls", C.c_int64), ("passes", C.c_int64),
         ("kernel_launches", C.c_int64), ("walk_launches", C.c_int64),
         ("evaluations", C.c_int64), ("interactions", C.c_int64),
+        ("walk1_ms", C.c_double), ("walk1_interactions", C.c_int64),
     ]
 
 

@@ -287,6 +287,7 @@ struct PhaseTimer : LoopHooks {
     marks.push_back(next++);
   }
   // marks come in groups of 4: before tree, after tree, after walk, after loop
+  int group = 0;  // pass groups collected in this call
   void collect() override
   {
     for (size_t i = 0; i + 3 < marks.size(); i += 4) {
@@ -297,6 +298,7 @@ struct PhaseTimer : LoopHooks {
       h->stats.tree_ms += a;
       h->stats.walk_ms += b;
       h->stats.loop_ms += c;
+      if (group++ == 0) h->stats.walk1_ms += b;
     }
     marks.clear();
     next = 2;
@@ -360,12 +362,13 @@ void pass_tree_and_energies(Ctx &c, LoopHooks *hk)
 void run_passes(Ctx &c, int max_passes, LoopHooks *hk)
 {
   const int max_chunks = c.N / kChunk + c.S + 1;
-  for (;;) {
+  for (int pass = 0;; pass++) {
     launch_plan(c, 0);
     launch_bbox_cube(c, max_chunks);
     read_plan(c);
     if (hk) hk->collect();
     const PassPlan pl = *c.plan_host;
+    if (pass == 1 && hk && hk->stats) hk->stats->walk1_interactions += pl.inter_done;
     launch_block_sort(c, pl.nsort_total, 0);  // unbound blocks of the previous pass
     if (pl.nactive == 0) break;
     if (hk && hk->stats) hk->stats->passes++;

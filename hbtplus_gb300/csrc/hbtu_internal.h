@@ -86,6 +86,7 @@ struct PassPlan {
   int nsort_total;  // elements of the unbound-part sort
   int nchunks_bound;
   int nrefine;
+  long long inter_done;  // walk interactions summed so far, all subhaloes
 };
 
 #define HBTU_CUDA(x)                                                        \

@@ -171,9 +171,19 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode)
   if (threadIdx.x == 0) nact = 0;
   __syncthreads();
   if (mode == 0) {
+    __shared__ unsigned long long inter;
+    if (threadIdx.x == 0) inter = 0;
+    __syncthreads();
     int cnt = 0;
-    for (int s = threadIdx.x; s < c.S; s += kPlanThreads) cnt += c.seg[s].status == SEG_ACTIVE;
+    unsigned long long it = 0;
+    for (int s = threadIdx.x; s < c.S; s += kPlanThreads) {
+      cnt += c.seg[s].status == SEG_ACTIVE;
+      it += (unsigned long long)c.seg[s].interactions;
+    }
     atomicAdd(&nact, cnt);
+    atomicAdd(&inter, it);
+    __syncthreads();
+    if (threadIdx.x == 0) c.plan->inter_done = (long long)inter;
     plan_scan4(c.S, get_pass, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
     if (threadIdx.x == 0) {
       c.plan->nactive = nact;

@@ -189,6 +189,8 @@ typedef struct hbtu_stats {
   int64_t walk_launches;   /* of which tree walks */
   int64_t evaluations;     /* target potentials evaluated */
   int64_t interactions;    /* tree-walk contributions summed */
+  double walk1_ms;         /* with timing on: the first pass's walk of each call */
+  int64_t walk1_interactions; /* contributions summed by those first-pass walks */
 } hbtu_stats;
 
 /* Turn per-phase device timing on (1) or off (0; the default).  With timing
