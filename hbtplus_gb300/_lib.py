@@ -93,6 +93,9 @@ SIGNATURES = {
     "hbtu_binding_energies": (C.c_int, [C.c_void_p, C.POINTER(hbtu_particles), C.c_int64,
                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "hbtu_last_error": (C.c_char_p, [C.c_void_p]),
+    "hbtu_energy_gradient": (C.c_int, [C.c_void_p, C.POINTER(hbtu_particles), C.c_int64,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]),
     "hbtu_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "hbtu_set_option": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     "hbtu_get_option": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int64)]),

@@ -120,6 +120,9 @@ static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
   sg.order = cv.take<long long>(N);
   sg.energy = cv.take<float>(N);
   sg.pot = cv.take<double>(N);
+  c.e_part = cv.take<double>(N);
+  sg.grad = cv.take<float>(7 * N);
+  sg.esum = cv.take<double>(S);
   sg.res = cv.take<hbtu_result>(S);
 }
 
@@ -223,6 +226,7 @@ hbtu_status setup_call(hbtu_handle *h, const hbtu_particles *p, long long S, con
   c.st = h->stream;
   c.plan_host = h->plan_host;
   c.pot_out = nullptr;
+  c.grad_pos = c.grad_vel = c.grad_mass = nullptr;
   const float *pos = p->pos, *vel = p->vel, *mass = p->mass;
   const long long *id = (const long long *)p->id;
   c.type = (int *)p->type;
@@ -617,6 +621,65 @@ hbtu_status hbtu_unbind(hbtu_handle *h, const hbtu_particles *p, int64_t n, cons
   if (n < 0) return fail(h, HBTU_ERR_INVALID_ARGUMENT, "negative particle count");
   const int64_t offsets[2] = {0, n};
   return hbtu_unbind_batch(h, p, 1, offsets, st, order_out, energy_out, res);
+}
+
+hbtu_status hbtu_energy_gradient(hbtu_handle *h, const hbtu_particles *p, int64_t nsub,
+                                 const int64_t *offsets, const hbtu_state *st, double *energy_out,
+                                 float *grad_pos, float *grad_vel, float *grad_mass)
+{
+  if (!h) return HBTU_ERR_INVALID_ARGUMENT;
+  if (nsub > 0 && !energy_out) return fail(h, HBTU_ERR_INVALID_ARGUMENT, "null energy_out");
+  try {
+    Ctx c;
+    Staging sg;
+    bool host = true;
+    // a single full pass over every particle: no sampling
+    const int64_t saved = h->params.max_sample_size;
+    h->params.max_sample_size = 0;
+    hbtu_status rc = setup_call(h, p, nsub, offsets, st, c, sg, host);
+    h->params.max_sample_size = saved;
+    if (rc != HBTU_OK) return rc;
+    if (nsub == 0) return HBTU_OK;
+    const long long N = c.N;
+    c.grad_pos = grad_pos ? (host ? sg.grad : grad_pos) : nullptr;
+    c.grad_vel = grad_vel ? (host ? sg.grad + 3 * N : grad_vel) : nullptr;
+    c.grad_mass = grad_mass ? (host ? sg.grad + 6 * N : grad_mass) : nullptr;
+    // every subhalo with at least one particle takes part (n == 1 included)
+    std::vector<SegState> segs(nsub);
+    HBTU_CUDA(cudaMemcpyAsync(segs.data(), c.seg, sizeof(SegState) * nsub, cudaMemcpyDeviceToHost,
+                              c.st));
+    HBTU_CUDA(cudaStreamSynchronize(c.st));
+    for (auto &g : segs)
+      if (g.n >= 1) g.status = SEG_ACTIVE;
+    HBTU_CUDA(cudaMemcpyAsync(c.seg, segs.data(), sizeof(SegState) * nsub, cudaMemcpyHostToDevice,
+                              c.st));
+    if (N > 0) HBTU_CUDA(cudaMemsetAsync(c.e_part, 0, sizeof(double) * N, c.st));
+    launch_plan(c, 0);
+    launch_bbox_cube(c, c.N / kChunk + c.S + 1);
+    read_plan(c);
+    const PassPlan pl = *c.plan_host;
+    launch_tree_build(c, pl);
+    launch_grad_walk(c, pl);
+    double *es = host ? sg.esum : energy_out;
+    launch_segment_sums(c, c.e_part, es);
+    if (host) {
+      HBTU_CUDA(cudaMemcpyAsync(energy_out, es, sizeof(double) * nsub, cudaMemcpyDeviceToHost,
+                                c.st));
+      if (grad_pos)
+        HBTU_CUDA(cudaMemcpyAsync(grad_pos, c.grad_pos, sizeof(float) * 3 * N,
+                                  cudaMemcpyDeviceToHost, c.st));
+      if (grad_vel)
+        HBTU_CUDA(cudaMemcpyAsync(grad_vel, c.grad_vel, sizeof(float) * 3 * N,
+                                  cudaMemcpyDeviceToHost, c.st));
+      if (grad_mass)
+        HBTU_CUDA(cudaMemcpyAsync(grad_mass, c.grad_mass, sizeof(float) * N,
+                                  cudaMemcpyDeviceToHost, c.st));
+    }
+    HBTU_CUDA(cudaStreamSynchronize(c.st));
+    return HBTU_OK;
+  } catch (const CudaError &e) {
+    return fail(h, HBTU_ERR_CUDA, e.what);
+  }
 }
 
 hbtu_status hbtu_binding_energies(hbtu_handle *h, const hbtu_particles *p, int64_t n,

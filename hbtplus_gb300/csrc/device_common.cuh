@@ -118,6 +118,9 @@ struct Ctx {
   int *Pk, *Qk;
   void *scan_tmp;
   double *pot_out;  // optional: potentials of a full pass (hbtu_binding_energies)
+  // adjoint outputs (hbtu_energy_gradient), by input position; grads may be null
+  float *grad_pos, *grad_vel, *grad_mass;
+  double *e_part;
 };
 
 // launchers (tree.cu)
@@ -125,6 +128,9 @@ void launch_bbox_cube(Ctx &c, int max_chunks);
 void launch_tree_build(Ctx &c, const PassPlan &pl);
 // launchers (walk.cu)
 void launch_walk(Ctx &c, const PassPlan &pl);
+void launch_grad_walk(Ctx &c, const PassPlan &pl);
+// per-subhalo sums of a per-particle double array (input positions), deterministic
+void launch_segment_sums(Ctx &c, const double *x, double *out);
 // launchers (loop.cu)
 void launch_init(Ctx &c, const float *pos, const float *vel, const float *mass,
                  const long long *id);

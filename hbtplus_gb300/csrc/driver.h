@@ -14,6 +14,8 @@ struct Staging {
   float *energy;
   double *pot;
   hbtu_result *res;
+  float *grad;   // 7 per particle: host-located gradient staging
+  double *esum;  // per subhalo
 };
 
 // Bytes of device workspace for N particles in S subhaloes, and the carving of

@@ -708,9 +708,57 @@ __global__ void __launch_bounds__(kLB) k_final_out(Ctx c, int64_t *order, float 
   }
 }
 
+// Deterministic per-subhalo sums of x[off_s .. off_s + n_s): one block per
+// 1024-element chunk (fixed-order tree), then the chunks of each subhalo in order.
+__global__ void __launch_bounds__(kLB) k_segsum_chunks(Ctx c, const double *x)
+{
+  const int b = blockIdx.x;
+  if (b >= c.bchunk_base[c.S]) return;
+  const int s = upper_bound_i(c.bchunk_base, c.S + 1, b) - 1;
+  const SegState &sg = c.seg[s];
+  const int lo = (b - c.bchunk_base[s]) * kChunk, hi = min(lo + kChunk, sg.n);
+  double v[1] = {0.};
+  for (int p = lo + threadIdx.x; p < hi; p += kLB) v[0] += x[sg.off + p];
+  block_sum<1>(v, c.chunk_sums + (size_t)b * kSums);
+}
+
+__global__ void k_segsum_combine(Ctx c, double *out)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= c.S) return;
+  double t = 0.;
+  for (int b = c.bchunk_base[s]; b < c.bchunk_base[s + 1]; b++) t += c.chunk_sums[(size_t)b * kSums];
+  out[s] = t;
+}
+
+__device__ int get_all_chunks(const Ctx &c, int s, int *v)
+{
+  v[0] = (c.seg[s].n + kChunk - 1) / kChunk;
+  v[1] = v[2] = v[3] = 0;
+  return 0;
+}
+
+__global__ void __launch_bounds__(kPlanThreads) k_plan_all(Ctx c)
+{
+  __shared__ int tot[4];
+  plan_scan4(c.S, get_all_chunks, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
+void launch_segment_sums(Ctx &c, const double *x, double *out)
+{
+  k_plan_all<<<1, kPlanThreads, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+  const int max_chunks = (c.N + kChunk - 1) / kChunk + c.S;
+  if (max_chunks > 0) {
+    k_segsum_chunks<<<max_chunks, kLB, 0, c.st>>>(c, x);
+    HBTU_LAUNCHED();
+  }
+  k_segsum_combine<<<nblk(c.S, 128), 128, 0, c.st>>>(c, out);
+  HBTU_LAUNCHED();
+}
 void launch_init(Ctx &c, const float *pos, const float *vel, const float *mass,
                  const long long *id)
 {

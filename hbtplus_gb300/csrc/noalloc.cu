@@ -131,6 +131,7 @@ extern "C" hbtu_status hbtu_unbind_noalloc(const hbtu_params *params, const hbtu
     c.st = (cudaStream_t)cuda_stream;
     c.plan_host = &plan_host;
     c.pot_out = nullptr;
+    c.grad_pos = c.grad_vel = c.grad_mass = nullptr;
     c.type = (int *)p->type;
     c.id = (long long *)p->id;
     c.opt_leaf_runs = 1;

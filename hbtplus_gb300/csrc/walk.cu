@@ -321,6 +321,102 @@ __global__ void __launch_bounds__(kWB) k_walk_fp64(Ctx c, int total)
   count_interactions(c, t.s, ninter);
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint: gradient of the total binding energy over a fixed particle set,
+//   E_tot = sum_i m_i |dv_i|^2 / 2 + (1/2) sum_i m_i phi_i,
+// with dv_i the velocity relative to the frame (RelativeVelocity, Hubble flow
+// included) and phi_i the walk potential (self term cancelled).  The frame is
+// the set's centre of mass, so its dependence on x, v, m cancels (sum m dv = 0):
+//   dE/dv_k = m_k dv_k,
+//   dE/dx_k = m_k (H a dv_k + grad phi(x_k)),
+//   dE/dm_k = |dv_k|^2 / 2 + phi_k.
+// grad phi is recomputed by a walk with the reference's opening rule on the same
+// tree (nothing of the energy walk is stored); per accepted node
+//   far  (r >= h): d(-m/r)/dx_t = -m dx / r^3,
+//   near (r < h):  d(m wp(u)/h)/dx_t = -m wp'(u) dx / (h^2 r),  u = r/h,
+// with wp' the derivative of the cubic-spline kernel; dx = x_node - x_target.
+__global__ void __launch_bounds__(kWB) k_grad_walk(Ctx c, int total)
+{
+  const DevParams &P = c.P;
+  const unsigned full = 0xffffffffu;
+  Target t;
+  load_target<true>(c, blockIdx.x * kWB + threadIdx.x, total, t);
+  double pot_d = (double)__fdiv_rn(t.mself, P.eps);
+  float pot_f = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
+  double axd = 0., ayd = 0., azd = 0.;
+  const float theta2 = P.theta2;
+  const float hf = (float)P.h, hinvf = (float)P.h_inv;
+  const double th2d = (double)P.theta2;
+  unsigned reduces = 0;
+  int cur = __reduce_min_sync(full, t.nxt);
+  while (cur != kDone) {
+    const float4 na = c.nd_rel[cur];
+    const int2 nm = c.nd_meta[cur];
+    if (t.nxt == cur) {
+      const float dx = na.x - t.q[0], dy = na.y - t.q[1], dz = na.z - t.q[2];
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (opens(na, t.q, __int_as_float(nm.x & 0x7fffffff), r2, theta2, th2d)) {
+        t.nxt = cur + 1 < t.end ? cur + 1 : kDone;
+      } else {
+        const int sk = nm.y;
+        t.nxt = (unsigned)(sk - cur - 1) < (unsigned)(t.end - cur - 1) ? sk : kDone;
+        const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
+        const float r = r2 * rinv;
+        float w;  // gradient weight: accel += m * w * dx
+        if (r >= hf) {
+          pot_f -= na.w * rinv;
+          w = rinv * rinv * rinv;
+        } else {
+          const float u = r * hinvf;
+          float wp, dwp;
+          if (u < 0.5f) {
+            wp = -2.8f + u * u * (5.333333333333f + u * u * (6.4f * u - 9.6f));
+            dwp = u * (10.666666666667f + u * u * (32.0f * u - 38.4f));
+          } else {
+            wp = -3.2f + 0.066666666667f / u +
+                 u * u * (10.666666666667f + u * (-16.0f + u * (9.6f - 2.133333333333f * u)));
+            dwp = -0.066666666667f / (u * u) +
+                  u * (21.333333333333f + u * (-48.0f + u * (38.4f - 10.666666666667f * u)));
+          }
+          pot_f += na.w * hinvf * wp;
+          w = r2 > 0.f ? hinvf * hinvf * dwp * rinv : 0.f;
+        }
+        const float mw = na.w * w;
+        ax += mw * dx;
+        ay += mw * dy;
+        az += mw * dz;
+      }
+    }
+    cur = __reduce_min_sync(full, t.nxt);
+    if ((++reduces & 15u) == 0u) {
+      pot_d += (double)pot_f;
+      axd += (double)ax;
+      ayd += (double)ay;
+      azd += (double)az;
+      pot_f = ax = ay = az = 0.f;
+    }
+  }
+  if (!t.active) return;
+  const SegState &sg = c.seg[t.s];
+  const double ga = ddiv((double)P.G, (double)P.a);
+  const double pot = dmul(dadd(pot_d, (double)pot_f), ga);
+  const double gphi[3] = {-ga * (axd + ax), -ga * (ayd + ay), -ga * (azd + az)};
+  const float4 a = c.pm[t.pid], v = c.vel[t.pid];
+  const float tp[3] = {a.x, a.y, a.z}, tv[3] = {v.x, v.y, v.z};
+  float dv[3];
+  relvel(tp, tv, sg.ref_pos, sg.ref_vel, dv, P);
+  const double m = (double)a.w;
+  const double k2 = (double)dv[0] * dv[0] + (double)dv[1] * dv[1] + (double)dv[2] * dv[2];
+  const double ha = (double)P.Hz * (double)P.a;
+  const int i = t.pid;  // no list permutation in this call: input position
+  if (c.grad_pos)
+    for (int j = 0; j < 3; j++) c.grad_pos[3 * i + j] = (float)(m * (ha * dv[j] + gphi[j]));
+  if (c.grad_vel)
+    for (int j = 0; j < 3; j++) c.grad_vel[3 * i + j] = (float)(m * dv[j]);
+  if (c.grad_mass) c.grad_mass[i] = (float)(0.5 * k2 + pot);
+  c.e_part[i] = 0.5 * m * k2 + 0.5 * m * pot;
+}
+
 }  // namespace
 
 void launch_walk(Ctx &c, const PassPlan &pl)
@@ -334,6 +430,14 @@ void launch_walk(Ctx &c, const PassPlan &pl)
     k_walk_fp32<true><<<blocks, kWB, 0, c.st>>>(c, n);
   else
     k_walk_fp32<false><<<blocks, kWB, 0, c.st>>>(c, n);
+  HBTU_LAUNCHED();
+}
+
+void launch_grad_walk(Ctx &c, const PassPlan &pl)
+{
+  const int n = pl.ntgt_total;
+  if (n <= 0) return;
+  k_grad_walk<<<(n + kWB - 1) / kWB, kWB, 0, c.st>>>(c, n);
   HBTU_LAUNCHED();
 }
 

@@ -205,6 +205,22 @@ hbtu_status hbtu_reset_stats(hbtu_handle *h);
 hbtu_status hbtu_set_option(hbtu_handle *h, const char *name, int64_t value);
 hbtu_status hbtu_get_option(const hbtu_handle *h, const char *name, int64_t *value);
 
+/* Adjoint of the binding energy: the gradient of each subhalo's total binding
+ * energy over a fixed particle set (e.g. its bound particles after unbinding),
+ *   E_tot = sum_i m_i |dv_i|^2 / 2 + 1/2 sum_i m_i phi_i,
+ * dv_i = RelativeVelocity(x_i, v_i, ref_pos, ref_vel) (src/snapshot.h:100-111),
+ * phi_i the tree potential of the unbinding walk (src/gravity_tree.cpp:79-164).
+ * No counterpart in the reference.  With the frame at the set's centre of mass:
+ *   dE/dv = m dv,  dE/dx = m (H a dv + grad phi),  dE/dm = |dv|^2 / 2 + phi,
+ * grad phi from a walk with the reference's opening rule (recomputed, nothing
+ * stored).  Batched like hbtu_unbind_batch: offsets (host), st[nsub] (host,
+ * ref_pos/ref_vel used), energy_out[nsub] double; grad_pos[3N], grad_vel[3N],
+ * grad_mass[N] float by input position, each may be NULL; arrays follow
+ * p->location. */
+hbtu_status hbtu_energy_gradient(hbtu_handle *h, const hbtu_particles *p, int64_t nsub,
+                                 const int64_t *offsets, const hbtu_state *st, double *energy_out,
+                                 float *grad_pos, float *grad_vel, float *grad_mass);
+
 /* Message of the last failed call on this handle (or of the last failed
  * hbtu_create when h is NULL). */
 const char *hbtu_last_error(const hbtu_handle *h);
