@@ -56,9 +56,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nsub", type=int, default=2000)
-    ap.add_argument("--workload", default="batch", choices=["batch", "single"],
+    ap.add_argument("--workload", default="batch", choices=["batch", "single", "host2e7"],
                     help="batch: the 2000-subhalo batch (default); single: the isolated "
-                         "1e5-particle NFW subhalo (+10%% contaminants)")
+                         "1e5-particle NFW subhalo (+10%% contaminants); host2e7: the "
+                         "2e7-particle host with 300 clumps (+5%% contaminants)")
+    ap.add_argument("--open-angle", type=float, default=0.45)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--leaf-runs", type=int, default=-1,
                     help="walk_leaf_runs option of the FP32 walk (-1: library default)")
@@ -74,12 +76,15 @@ def dist_env():
     return ws, rank, local
 
 
-def workload(nsub: int, rank: int, kind: str = "batch"):
+def workload(nsub: int, rank: int, kind: str = "batch", theta: float = 0.45):
     from hbtplus_gb300 import synthetic as S
+    p = S.default_params(open_angle=theta)
     if kind == "single":
-        return S.concat([S.single_subhalo(seed=20261203 + 1000 * rank)]), S.default_params()
+        return S.concat([S.single_subhalo(seed=20261203 + 1000 * rank)]), p
+    if kind == "host2e7":
+        return S.concat([S.host_with_clumps(seed=20261205 + 1000 * rank)]), p
     b = S.subhalo_batch(nsub=nsub, seed=20261204 + 1000 * rank)
-    return b, S.default_params()
+    return b, p
 
 
 def cpu_threads() -> int:
@@ -173,7 +178,7 @@ def measured_peaks():
 def run_reference_arm(args, ws, rank):
     if rank != 0:
         return
-    batch, params = workload(args.nsub, 0, args.workload)
+    batch, params = workload(args.nsub, 0, args.workload, args.open_angle)
     threads = cpu_threads()
     for _ in range(args.warmup):
         cpu_reference_time(params, batch, threads)
@@ -204,13 +209,16 @@ def config_of(args, batch):
     if args.workload == "single":
         name = ("single subhalo: 1e5-particle NFW (r200 0.2 Mpc/h, c 10) + 10% contaminants, "
                 "100 Mpc/h periodic box")
+    elif args.workload == "host2e7":
+        name = ("large host: 2e7-particle NFW (r200 1 Mpc/h, c 5) + 300 Plummer clumps "
+                "(1e3-1e5 particles) + 5% contaminants, 100 Mpc/h periodic box")
     else:
         name = (f"{nsub}-subhalo batch: dN/dlnN ~ N^-0.9 on [20, 2e5], NFW + Jeans, "
                 "20% contaminants, 100 Mpc/h periodic box")
     return {"workload": name,
             "nsub": nsub, "particles": int(batch["offsets"][-1]),
             "max_subhalo": int(np.max(np.diff(batch["offsets"]))),
-            "softening": 0.002, "open_angle": 0.45, "max_sample_size": 0,
+            "softening": 0.002, "open_angle": args.open_angle, "max_sample_size": 0,
             "precision": args.precision, "walk_leaf_runs": args.leaf_runs if args.leaf_runs >= 0 else 1,
             "l2": "flushed before each timed step (256 MB write)"}
 
@@ -234,7 +242,7 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    batch, params = workload(args.nsub, rank, args.workload)
+    batch, params = workload(args.nsub, rank, args.workload, args.open_angle)
     nsub = len(batch["offsets"]) - 1
     ntot = int(batch["offsets"][-1])
     prec = 1 if args.precision == "fp64" else 0
@@ -372,7 +380,7 @@ def main():
 
     # -- plain form: one subhalo per call on the same GB300 ------------------------
     plain = None
-    if not args.no_plain:
+    if not args.no_plain and nsub > 1:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         order_np = np.empty(ntot, np.int64)
@@ -403,6 +411,8 @@ def main():
     # -- CPU baseline (reference path on this host's cores) and accuracy ----------------
     cpu = None
     accuracy = None
+    if args.workload == "host2e7":
+        args.no_cpu = True  # the CPU path needs several minutes per unbinding of 2.7e7 particles
     if not args.no_cpu:
         threads = cpu_threads()
         t_cpu, kind, cres = cpu_reference_time(params, batch, threads)

@@ -93,6 +93,8 @@ SIGNATURES = {
     "hbtu_binding_energies": (C.c_int, [C.c_void_p, C.POINTER(hbtu_particles), C.c_int64,
                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "hbtu_last_error": (C.c_char_p, [C.c_void_p]),
+    "hbtu_direct_potential": (C.c_int, [C.c_void_p, C.POINTER(hbtu_particles), C.c_int64,
+                                        C.c_void_p, C.c_int64, C.c_void_p]),
     "hbtu_energy_gradient": (C.c_int, [C.c_void_p, C.POINTER(hbtu_particles), C.c_int64,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p]),

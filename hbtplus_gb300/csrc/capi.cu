@@ -682,6 +682,58 @@ hbtu_status hbtu_energy_gradient(hbtu_handle *h, const hbtu_particles *p, int64_
   }
 }
 
+hbtu_status hbtu_direct_potential(hbtu_handle *h, const hbtu_particles *p, int64_t n,
+                                  const int64_t *targets, int64_t ntarget, double *potential_out)
+{
+  if (!h) return HBTU_ERR_INVALID_ARGUMENT;
+  if (n < 0 || ntarget < 0 || (ntarget > 0 && (!targets || !potential_out)))
+    return fail(h, HBTU_ERR_INVALID_ARGUMENT, "bad count, target list or output pointer");
+  for (int64_t k = 0; k < ntarget; k++)
+    if (targets[k] < 0 || targets[k] >= n)
+      return fail(h, HBTU_ERR_INVALID_ARGUMENT, "target index out of range");
+  int *d_t = nullptr;
+  double *d_out = nullptr, *d_part = nullptr;
+  try {
+    hbtu_state st;
+    memset(&st, 0, sizeof(st));
+    st.mostbound_id = -1;
+    const int64_t offsets[2] = {0, n};
+    Ctx c;
+    Staging sg;
+    bool host = true;
+    hbtu_status rc = setup_call(h, p, 1, offsets, &st, c, sg, host);
+    if (rc != HBTU_OK) return rc;
+    if (ntarget == 0) return HBTU_OK;
+    const int tiles = (int)((ntarget + 127) / 128);
+    const int nsplit = std::max(1, std::min(512, (16 * 152 + tiles - 1) / tiles));
+    std::vector<int> t32(targets, targets + ntarget);
+    if (cudaMalloc(&d_t, sizeof(int) * ntarget) != cudaSuccess ||
+        cudaMalloc(&d_out, sizeof(double) * ntarget) != cudaSuccess ||
+        cudaMalloc(&d_part, sizeof(double) * ntarget * nsplit) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(d_t);
+      cudaFree(d_out);
+      cudaFree(d_part);
+      return fail(h, HBTU_ERR_OUT_OF_MEMORY, "direct potential buffers");
+    }
+    HBTU_CUDA(cudaMemcpyAsync(d_t, t32.data(), sizeof(int) * ntarget, cudaMemcpyHostToDevice,
+                              c.st));
+    direct_potential_fp64(c.P, c.pm, c.N, d_t, (int)ntarget, d_out, d_part, nsplit, c.st);
+    HBTU_CUDA(cudaMemcpyAsync(potential_out, d_out, sizeof(double) * ntarget,
+                              host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, c.st));
+    HBTU_CUDA(cudaStreamSynchronize(c.st));
+    cudaFree(d_t);
+    cudaFree(d_out);
+    cudaFree(d_part);
+    return HBTU_OK;
+  } catch (const CudaError &e) {
+    cudaFree(d_t);
+    cudaFree(d_out);
+    cudaFree(d_part);
+    return fail(h, HBTU_ERR_CUDA, e.what);
+  }
+}
+
 hbtu_status hbtu_binding_energies(hbtu_handle *h, const hbtu_particles *p, int64_t n,
                                   const float ref_pos[3], const float ref_vel[3],
                                   float *energy_out, double *potential_out)

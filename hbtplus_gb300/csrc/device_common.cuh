@@ -131,6 +131,9 @@ void launch_walk(Ctx &c, const PassPlan &pl);
 void launch_grad_walk(Ctx &c, const PassPlan &pl);
 // per-subhalo sums of a per-particle double array (input positions), deterministic
 void launch_segment_sums(Ctx &c, const double *x, double *out);
+// (direct.cu) exact FP64 potentials of particles tidx[0..nt) from all n particles
+void direct_potential_fp64(const DevParams &P, const float4 *pm, int n, const int *tidx, int nt,
+                           double *out, double *partial, int nsplit, cudaStream_t st);
 // launchers (loop.cu)
 void launch_init(Ctx &c, const float *pos, const float *vel, const float *mass,
                  const long long *id);

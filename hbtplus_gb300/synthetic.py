@@ -15,6 +15,8 @@ Workloads (numpy.random.Generator(PCG64), seed 20261203 + index):
   subhalo_batch()   2000 subhaloes, N from dN/dlnN ~ N^-0.9 on [20, 2e5],
                     c ~ U(5, 20), r200 = 0.2 (N/1e5)^(1/3), 20% contaminants,
                     about 5% of centres within r200 of a box face.
+  host_with_clumps() a 2e7-particle NFW host (r200 = 1, c = 5) with 300 Plummer
+                    clumps (1e3-1e5 particles, a = 0.01) and 5% contaminants.
 
 A subhalo is a dict with id (int64), pos/vel (n,3 float32), mass, type
 (int32), ref_pos/ref_vel (initial frame), mostbound_pos/mostbound_vel
@@ -128,6 +130,73 @@ def single_subhalo(n: int = 100_000, seed: int = 20261203, r200: float = 0.2, c:
     rng = np.random.Generator(np.random.PCG64(seed))
     sub = nfw_subhalo(rng, n, r200, c, contaminant_frac=contaminant_frac, box=box)
     _assign_ids(rng, [sub])
+    return sub
+
+
+def plummer(rng, n: int, a: float, m: float = 1e-4, rmax_factor: float = 10.0):
+    """Plummer sphere of n particles (scale radius a, truncated at rmax_factor*a)
+    with isotropic Gaussian velocities, sigma^2(r) = G M / (6 sqrt(r^2 + a^2))."""
+    mt = n * m
+    fmax = rmax_factor ** 3 / (1.0 + rmax_factor ** 2) ** 1.5  # mass fraction inside rmax
+    u = rng.uniform(size=n) * fmax
+    r = a / np.sqrt(u ** (-2.0 / 3.0) - 1.0)
+    pos = _unit_vectors(rng, n) * r[:, None]
+    sig = np.sqrt(G_MPC_KMS * mt / (6.0 * np.sqrt(r * r + a * a)))
+    vel = rng.normal(size=(n, 3)) * sig[:, None]
+    return pos, vel
+
+
+def host_with_clumps(n_host: int = 20_000_000, r200: float = 1.0, c: float = 5.0,
+                     nclumps: int = 300, clump_min: float = 1e3, clump_max: float = 1e5,
+                     clump_a: float = 0.01, contaminant_frac: float = 0.05,
+                     seed: int = 20261205, box: float = 100.0, m: float = 1e-4) -> dict:
+    """Large host subhalo: NFW host (r200 = 1 Mpc/h, c = 5) with Jeans velocities,
+    nclumps Plummer satellites (sizes log-uniform in [1e3, 1e5], scale radius
+    0.01 Mpc/h) placed on the host profile with orbital velocities drawn from the
+    host's dispersion there, plus unbound contaminants (5% of the total)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    rs = r200 / c
+    mtot_host = n_host * m
+    x, menc, sig2, phi = _nfw_profile_tables(c)
+    xr = np.interp(rng.uniform(size=n_host), menc, x)
+    pos = [(_unit_vectors(rng, n_host) * (xr * rs)[:, None]).astype(np.float64)]
+    sig = np.sqrt(np.maximum(np.interp(xr, x, sig2), 0.0) * G_MPC_KMS * mtot_host / rs)
+    vel = [rng.normal(size=(n_host, 3)) * sig[:, None]]
+    del xr, sig
+    sizes = np.exp(rng.uniform(np.log(clump_min), np.log(clump_max), size=nclumps)).astype(np.int64)
+    for k in range(nclumps):
+        xc = np.interp(rng.uniform(0.05, 0.95), menc, x)
+        cpos = _unit_vectors(rng, 1)[0] * xc * rs
+        csig = np.sqrt(max(np.interp(xc, x, sig2), 0.0) * G_MPC_KMS * mtot_host / rs)
+        cvel = rng.normal(size=3) * csig
+        p, v = plummer(rng, int(sizes[k]), clump_a, m)
+        pos.append(p + cpos)
+        vel.append(v + cvel)
+    n_in = n_host + int(sizes.sum())
+    ncont = int(round(contaminant_frac / (1.0 - contaminant_frac) * n_in))
+    rc = 2.0 * r200 * rng.uniform(size=ncont) ** (1.0 / 3.0)
+    xcn = rc / rs
+    phic = np.where(xcn <= c, np.interp(np.minimum(xcn, c), x, phi) * G_MPC_KMS * mtot_host / rs,
+                    -G_MPC_KMS * mtot_host / np.maximum(rc, 1e-12))
+    pos.append(_unit_vectors(rng, ncont) * rc[:, None])
+    vel.append(_unit_vectors(rng, ncont) * (3.0 * np.sqrt(2.0 * np.abs(phic)))[:, None])
+    pos = np.concatenate(pos)
+    vel = np.concatenate(vel)
+    center = rng.uniform(0.0, box, size=3)
+    k0 = int(np.argmin(np.einsum("ij,ij->i", pos, pos)))
+    pos[[0, k0]] = pos[[k0, 0]]
+    vel[[0, k0]] = vel[[k0, 0]]
+    pos32 = np.mod(pos + center, box).astype(np.float32)
+    pos32 = np.where(pos32 >= np.float32(box), np.float32(0.0), pos32)
+    del pos
+    ntot = len(pos32)
+    sub = dict(pos=pos32, vel=vel.astype(np.float32), mass=np.full(ntot, m, np.float32),
+               type=np.ones(ntot, np.int32), ref_pos=center.astype(np.float32),
+               ref_vel=np.zeros(3, np.float32))
+    sub["mostbound_pos"] = sub["pos"][0].copy()
+    sub["mostbound_vel"] = sub["vel"][0].copy()
+    sub["id"] = rng.permutation(ntot).astype(np.int64)
+    sub["mostbound_id"] = int(sub["id"][0])
     return sub
 
 

@@ -282,6 +282,21 @@ class Unbinder:
         del keep
         return E[:n], pot[:n]
 
+    def direct_potential(self, pos, mass, targets, vel=None, ids=None):
+        """Exact FP64 pairwise potentials (G/a included) of particles `targets`
+        from all particles: the quantity the tree walk approximates."""
+        n = len(mass)
+        d = dict(id=ids if ids is not None else np.arange(n, dtype=np.int64), pos=pos,
+                 vel=vel if vel is not None else np.zeros((n, 3), np.float32), mass=mass)
+        p, keep = self._host_particles(d)
+        t = np.ascontiguousarray(targets, np.int64)
+        out = np.zeros(max(len(t), 1), np.float64)
+        rc = self.lib.hbtu_direct_potential(self.handle, C.byref(p), n, _ptr(t), len(t),
+                                            _ptr(out))
+        _lib.check(rc, self.handle)
+        del keep
+        return out[:len(t)]
+
     # -- device-resident calls (torch tensors on the handle's device) --------
     def unbind_batch_device(self, dev: dict, offsets: np.ndarray, states, out: dict):
         """Batch call on device-resident torch tensors.  ``dev`` holds id, pos,

@@ -221,6 +221,15 @@ hbtu_status hbtu_energy_gradient(hbtu_handle *h, const hbtu_particles *p, int64_
                                  const int64_t *offsets, const hbtu_state *st, double *energy_out,
                                  float *grad_pos, float *grad_vel, float *grad_mass);
 
+/* Validation utility (no counterpart in the reference): exact pairwise
+ * potentials in FP64 of the particles targets[0..ntarget) (indices into p)
+ * from all n particles of p, with the reference's spline softening and
+ * periodic wrap, times G/a -- the quantity GravityTree_t::EvaluatePotential
+ * approximates (src/gravity_tree.cpp:79-164).  targets and potential_out are
+ * host memory; p follows p->location. */
+hbtu_status hbtu_direct_potential(hbtu_handle *h, const hbtu_particles *p, int64_t n,
+                                  const int64_t *targets, int64_t ntarget, double *potential_out);
+
 /* Message of the last failed call on this handle (or of the last failed
  * hbtu_create when h is NULL). */
 const char *hbtu_last_error(const hbtu_handle *h);
