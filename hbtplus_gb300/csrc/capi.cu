@@ -32,6 +32,7 @@ struct hbtu_handle {
   bool timing = false;
   // tuning options (hbtu_set_option)
   int64_t opt_leaf_runs = 1;
+  int64_t opt_schedule = 0;
   std::vector<cudaEvent_t> events;  // pool: 4 per pass when timing, 2 per call
 };
 
@@ -106,8 +107,7 @@ static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
   c.X = cv.take<long long>(N + 1);
   // one spare slot: the walk prefetches node cur+1 speculatively
   c.nd_abs = cv.take<float4>(2 * N + 1);
-  c.nd_rel = cv.take<float4>(2 * N + 1);
-  c.nd_meta = cv.take<int2>(2 * N + 1);
+  c.nd = cv.take<WNode>(2 * N + 1);
   c.pcode = cv.take<long long>(N + 1);
   c.pX = cv.take<long long>(N + 1);
   c.Pk = cv.take<int>(N);
@@ -246,6 +246,7 @@ hbtu_status setup_call(hbtu_handle *h, const hbtu_particles *p, long long S, con
   }
   c.id = (long long *)id;
   c.opt_leaf_runs = (int)h->opt_leaf_runs;
+  c.opt_schedule = (int)h->opt_schedule;
   std::vector<SegState> segs;
   std::vector<int> segoff, order(S);
   init_states(h, S, offsets, st, segs, segoff);
@@ -513,6 +514,11 @@ hbtu_status hbtu_set_option(hbtu_handle *h, const char *name, int64_t value)
     h->opt_leaf_runs = value;
     return HBTU_OK;
   }
+  if (n == "walk_schedule") {
+    if (value != 0 && value != 1) return fail(h, HBTU_ERR_INVALID_ARGUMENT, "walk_schedule: 0 or 1");
+    h->opt_schedule = value;
+    return HBTU_OK;
+  }
   return fail(h, HBTU_ERR_INVALID_ARGUMENT, "unknown option " + n);
 }
 
@@ -522,6 +528,10 @@ hbtu_status hbtu_get_option(const hbtu_handle *h, const char *name, int64_t *val
   const std::string n(name);
   if (n == "walk_leaf_runs") {
     *value = h->opt_leaf_runs;
+    return HBTU_OK;
+  }
+  if (n == "walk_schedule") {
+    *value = h->opt_schedule;
     return HBTU_OK;
   }
   return HBTU_ERR_INVALID_ARGUMENT;

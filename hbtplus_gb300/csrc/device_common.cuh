@@ -13,6 +13,30 @@ namespace hbtu {
 constexpr int kChunk = 1024;  // elements per reduction chunk
 constexpr int kDone = 0x7fffffff;
 
+// One tree node as the walks read it (32 bytes, one sector): p = {x, y, z,
+// mass} relative to the frame centre (sign bit of the mass set on cells),
+// m = {len*len bits with the all-particle-children flag in the sign bit, skip
+// pointer, sure-open and sure-accept squared distances as float bits}.
+struct __align__(32) WNode {
+  float4 p;
+  int4 m;
+};
+
+// Both halves of node i in one 256-bit load.
+__device__ __forceinline__ void load_node(const WNode *nd, int i, float4 &p, int4 &m)
+{
+  asm("ld.global.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w), "=r"(m.x), "=r"(m.y), "=r"(m.z), "=r"(m.w)
+      : "l"(nd + i));
+}
+
+__device__ __forceinline__ void load_node(const WNode *nd, int i, float4 &p, int2 &m)
+{
+  int4 q;
+  load_node(nd, i, p, q);
+  m = make_int2(q.x, q.y);
+}
+
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
@@ -99,7 +123,8 @@ struct Ctx {
   int *tchunk_base, *bchunk_base, *ub_base;  // S+1 each
   int *seg_off;                              // S+1
   int *seg_order;                            // S: subhaloes by size, largest first
-  int opt_leaf_runs;                         // FP32 walk streams all-particle cells
+  int opt_leaf_runs;                         // warp schedule streams all-particle cells
+  int opt_schedule;                          // FP32 walk: 0 one walk per lane, 1 warp schedule
   int *part_info;                            // 8 ints per segment
   unsigned *chunk_bbox;                      // 6 per chunk
   double *chunk_sums;                        // 16 per chunk
@@ -111,8 +136,8 @@ struct Ctx {
   unsigned long long *mask;
   long long *X;
   // nodes (2 per tree particle)
-  float4 *nd_abs, *nd_rel;
-  int2 *nd_meta;  // {len*len as float bits (0 for particles), skip pointer}
+  float4 *nd_abs;
+  WNode *nd;
   // partition
   long long *pcode, *pX;
   int *Pk, *Qk;

@@ -11,11 +11,13 @@
 //   tree        per segment 2*ntree node slots in DFS preorder:
 //               nd_abs  float4 {x, y, z, m} absolute centre of mass (float,
 //                       as the reference stores TreeCell_t::way.s)
-//               nd_rel  float4 {x, y, z, m} same, relative to the segment's
-//                       frame centre, wrapped once in double then cast
-//               nd_meta int2   {len*len of the cell as float bits (0 for
-//                       particle leaves; sign bit set on cells whose children
-//                       are all particles), next node after the subtree}
+//               nd      WNode  32-byte record read by the walks in one load:
+//                       p = {x, y, z, m} relative to the segment's frame
+//                       centre (wrapped once in double, then cast);
+//                       m = {len*len of the cell as float bits (0 for particle
+//                       leaves; sign bit set on cells whose children are all
+//                       particles), next node after the subtree (kDone when
+//                       the subtree ends the tree), 0, 0}
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

@@ -135,6 +135,7 @@ extern "C" hbtu_status hbtu_unbind_noalloc(const hbtu_params *params, const hbtu
     c.type = (int *)p->type;
     c.id = (long long *)p->id;
     c.opt_leaf_runs = 1;
+    c.opt_schedule = 0;
     SegState g;
     init_segment(g, 0, (int)n, *st, params->max_sample_size);
     const int segoff[2] = {0, (int)n};

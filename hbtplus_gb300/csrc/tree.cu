@@ -16,7 +16,8 @@
 //      cells where a key prefix branches.  A cell with one child cell has the
 //      same mass and centre of mass as that child (exact in double), so the
 //      collapsed cell, given the smaller child's side, makes the same walk;
-//   5. DFS preorder numbering and skip pointers from prefix counts;
+//   5. DFS preorder numbering and skip pointers from prefix counts (a skip
+//      pointer that leaves the tree is stored as kDone);
 //   6. bottom-up mass and centre of mass over each cell's children in octant
 //      order, in double, rounded to float per cell as the reference does
 //      (ProcessNode / FillNodeCenter, src/gravity_tree.cpp:18-46).
@@ -227,6 +228,23 @@ __global__ void __launch_bounds__(kTB) k_popc(Ctx c, int ntotal)
   c.pcode[e] = e < ntotal ? __popcll(c.mask[e]) : 0;
 }
 
+// Walk record meta of a cell with side^2 = l2 (float, as the reference
+// computes len*len): the squared distances below which the cell surely opens
+// and above which it surely does not, l2/theta^2 (1 -+ 1e-5); in between the
+// walk takes the reference's decision in double.  Particles (never opened)
+// get -1 for both.
+__device__ __forceinline__ int4 cell_meta(float l2, int skip, const DevParams &P)
+{
+  const double q = (double)l2 / (double)P.theta2;
+  const float lo = (float)(q * (1.0 - 1e-5)), hi = (float)(q * (1.0 + 1e-5));
+  return make_int4(__float_as_int(l2), skip, __float_as_int(lo), __float_as_int(hi));
+}
+
+__device__ __forceinline__ int4 particle_meta(int skip)
+{
+  return make_int4(0, skip, __float_as_int(-1.f), __float_as_int(-1.f));
+}
+
 __device__ __forceinline__ float4 make_rel(float4 a, const float fc[3], const DevParams &P)
 {
   return make_float4(rel_coord(a.x, fc[0], P), rel_coord(a.y, fc[1], P), rel_coord(a.z, fc[2], P),
@@ -248,20 +266,21 @@ __global__ void __launch_bounds__(kTB) k_leaves(Ctx c, int ntotal)
   if (n == 1) {  // a root cell of side 0 holding the particle (tpp:56-102 with one particle)
     const float4 r = make_rel(a, sg.fc, c.P);
     c.nd_abs[nb] = a;
-    c.nd_rel[nb] = r;
-    c.nd_meta[nb] = make_int2(__float_as_int(fmul((float)sg.len, (float)sg.len)), nb + 2);
+    c.nd[nb].p = make_float4(r.x, r.y, r.z, -r.w);  // the sign bit marks a cell
+    c.nd[nb].m = cell_meta(fmul((float)sg.len, (float)sg.len), kDone, c.P);
     c.nd_abs[nb + 1] = a;
-    c.nd_rel[nb + 1] = r;
-    c.nd_meta[nb + 1] = make_int2(0, nb + 2);
+    c.nd[nb + 1].p = r;
+    c.nd[nb + 1].m = particle_meta(kDone);
     sg.nnodes = 2;
     return;
   }
   const long long xb = c.X[base];
   const int idx = j + (int)(c.X[e + 1] - xb);
+  const int nnodes = n + (int)(c.X[base + n] - xb);
   c.nd_abs[nb + idx] = a;
-  c.nd_rel[nb + idx] = make_rel(a, sg.fc, c.P);
-  c.nd_meta[nb + idx] = make_int2(0, nb + idx + 1);
-  if (j == 0) sg.nnodes = n + (int)(c.X[base + n] - xb);
+  c.nd[nb + idx].p = make_rel(a, sg.fc, c.P);
+  c.nd[nb + idx].m = particle_meta(idx + 1 < nnodes ? nb + idx + 1 : kDone);
+  if (j == 0) sg.nnodes = nnodes;
 }
 
 // Cells: preorder index, skip pointer, side (len*len in float), parent cell.
@@ -284,7 +303,8 @@ __global__ void __launch_bounds__(kTB) k_cellnodes(Ctx c, int ntotal)
   for (int k = 0; k < od; k++)
     if (len >= (double)c.P.res) len = dmul(len, 0.5);
   const float lf = (float)len;
-  c.nd_meta[nb + idx] = make_int2(__float_as_int(fmul(lf, lf)), nb + skip);
+  const int n = c.tree_base[s + 1] - base;
+  c.nd[nb + idx].m = cell_meta(fmul(lf, lf), hi + 1 < n ? nb + skip : kDone, c.P);
   c.cidx[e] = nb + idx;
   c.cskip[e] = nb + skip;
   int p = c.parentI[e];
@@ -304,8 +324,8 @@ __global__ void __launch_bounds__(kTB) k_moments(Ctx c, int ntotal)
   const SegState &sg = c.seg[s];
   {
     // a cell without child cells: mark it for the walk's leaf runs (sign bit of len*len)
-    int2 *meta = &c.nd_meta[c.cidx[e]];
-    meta->x = meta->x | (int)0x80000000;
+    int *meta = &c.nd[c.cidx[e]].m.x;
+    *meta = *meta | (int)0x80000000;
   }
   for (int level = 0; level <= 2 * kMaxLevels + 2; level++) {
     const int idx = c.cidx[e], end = c.cskip[e];
@@ -317,13 +337,15 @@ __global__ void __launch_bounds__(kTB) k_moments(Ctx c, int ntotal)
       cx = dadd(cx, dmul((double)a.x, w));
       cy = dadd(cy, dmul((double)a.y, w));
       cz = dadd(cz, dmul((double)a.z, w));
-      const int nk = c.nd_meta[k].y;
+      const int nk = c.nd[k].m.y;
       k = nk > k ? nk : end;  // skip pointers always move forward
     }
     const float4 r = make_float4(__double2float_rn(ddiv(cx, m)), __double2float_rn(ddiv(cy, m)),
                                  __double2float_rn(ddiv(cz, m)), __double2float_rn(m));
     __stcg(&c.nd_abs[idx], r);
-    c.nd_rel[idx] = make_rel(r, sg.fc, c.P);
+    float4 rel = make_rel(r, sg.fc, c.P);
+    rel.w = -rel.w;  // the sign bit marks a cell for the walks
+    c.nd[idx].p = rel;
     __threadfence();
     const int p = c.pcell[e];
     if (p < 0) break;

@@ -7,21 +7,20 @@
 // Each target performs exactly the reference's stackless walk: at a cell it
 // opens (goes to the first child, preorder index + 1) when
 // len*len > r*r*theta^2, otherwise it takes the cell's monopole and jumps to
-// the skip pointer.  A warp walks its targets together: it visits the
-// smallest preorder index any of its targets still needs, so a node is
-// fetched once per warp as a broadcast and every target sums its own
-// interactions in its own reference order.  When some target opens the
-// current node, the next node is exactly cur + 1 (children follow their cell
-// in preorder, every other target is already past cur), so that step needs no
-// warp reduction and its node was prefetched one step earlier.  Targets are
-// taken in Morton order, subhaloes largest first.
+// the skip pointer; particles are never opened.  Targets are taken in Morton
+// order, subhaloes largest first, so a warp holds neighbouring targets.
 //
 // FP32 (default): coordinates relative to the subhalo frame centre, wrapped
 // once in double, so the per-interaction periodic wrap disappears; opening
 // decisions within 1e-5 of the threshold are re-taken in double exactly as
-// the reference takes them; the potential is summed in float and flushed into
-// a double regularly.  Cells whose children are all particles are streamed
-// (leaf runs, below).
+// the reference takes them; the potential is summed in float with
+// compensation and formed in double once per target (no double arithmetic in
+// the loop: this GPU's FP64 rate is 1/64 of its FP32 rate).  Two schedules:
+//   lane (default): every lane walks its own target, one 32-byte node record
+//     per step; large blocks keep a block's neighbouring targets on one SM,
+//     so the walks share L1;
+//   warp: the warp visits the smallest index any of its targets waits at, so
+//     each node is a broadcast load (kept as an option for comparison).
 // FP64: absolute float coordinates, NEAREST per interaction, every operation
 // in the reference's order without fused multiply-add.
 #include "device_common.cuh"
@@ -134,26 +133,6 @@ __device__ __forceinline__ void count_interactions(const Ctx &c, int s, int n)
   }
 }
 
-// Softened potential of one interaction in FP32, added into pot_f.
-__device__ __forceinline__ void interact_fp32(float4 na, float r2, float &pot_f, float hf,
-                                              float hinvf)
-{
-  const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
-  const float r = r2 * rinv;
-  if (r >= hf) {
-    pot_f -= na.w * rinv;
-  } else {  // cubic-spline softened potential (Springel, Yoshida & White 2001)
-    const float u = r * hinvf;
-    float wp;
-    if (u < 0.5f)
-      wp = -2.8f + u * u * (5.333333333333f + u * u * (6.4f * u - 9.6f));
-    else
-      wp = -3.2f + 0.066666666667f / u +
-           u * u * (10.666666666667f + u * (-16.0f + u * (9.6f - 2.133333333333f * u)));
-    pot_f += na.w * hinvf * wp;
-  }
-}
-
 // Opening test of the reference, len*len > r*r*theta^2: float first, and in
 // double with the reference's operation order when within 1e-5 of the edge.
 __device__ __forceinline__ bool opens(float4 na, const float q[3], float l2, float r2, float theta2,
@@ -161,7 +140,7 @@ __device__ __forceinline__ bool opens(float4 na, const float q[3], float l2, flo
 {
   const float thr = r2 * theta2;
   bool open = l2 > thr;
-  if (fabsf(l2 - thr) <= 1e-5f * thr) {
+  if (l2 > 0.f && fabsf(l2 - thr) <= 1e-5f * thr) {  // particles (l2 = 0) never open
     const double ex = dsub((double)na.x, (double)q[0]);
     const double ey = dsub((double)na.y, (double)q[1]);
     const double ez = dsub((double)na.z, (double)q[2]);
@@ -177,10 +156,57 @@ __device__ __forceinline__ float dist2(float4 na, const float q[3])
   return dx * dx + dy * dy + dz * dz;
 }
 
-// FP32 walk.  Leaf runs: when targets open a cell whose children are all
-// particles, each of those targets takes every child in order (particles are
-// never opened) -- the warp streams the children through a loop with no
-// opening test and no scheduling per node.
+// FP32 potential sum without double arithmetic in the walk loop (this GPU's
+// FP64 rate is 1/64 of its FP32 rate): interactions go into a short float
+// partial sum `f`, which is flushed every few steps into a compensated
+// (Kahan) float total hi - c.  The total is formed in double once per target.
+struct PotAcc {
+  float f = 0.f, hi = 0.f, c = 0.f;
+  __device__ __forceinline__ void flush()
+  {
+    const float y = __fsub_rn(f, c);
+    const float t = __fadd_rn(hi, y);
+    c = __fsub_rn(__fsub_rn(t, hi), y);
+    hi = t;
+    f = 0.f;
+  }
+  __device__ __forceinline__ double total(double base) const
+  {
+    return dadd(dadd(base, (double)hi), dsub((double)f, (double)c));
+  }
+};
+
+// Softened potential without a division: 1/u = h/r = h * rinv.
+__device__ __forceinline__ float softened_fp32(float m, float r2, float rinv, float hf, float hinvf)
+{
+  const float r = r2 * rinv;
+  const float u = r * hinvf;
+  float wp;
+  if (u < 0.5f)
+    wp = -2.8f + u * u * (5.333333333333f + u * u * (6.4f * u - 9.6f));
+  else
+    wp = -3.2f + 0.066666666667f * (hf * rinv) +
+         u * u * (10.666666666667f + u * (-16.0f + u * (9.6f - 2.133333333333f * u)));
+  return m * hinvf * wp;
+}
+
+// One monopole interaction in FP32: -m/r outside the softening length h,
+// the cubic-spline potential inside it (Springel, Yoshida & White 2001).
+__device__ __forceinline__ void interact(float4 na, float r2, float &pot_f, float hf, float h2f,
+                                         float hinvf)
+{
+  const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
+  const float m = fabsf(na.w);  // cells carry their mass with the sign bit set
+  if (r2 >= h2f)
+    pot_f = fmaf(-m, rinv, pot_f);
+  else
+    pot_f += softened_fp32(m, r2, rinv, hf, hinvf);
+}
+
+// FP32 walk, warp schedule.  Leaf runs: when targets open a cell
+// whose children are all particles, each of those targets takes every child
+// in order (particles are never opened) -- the warp streams the children
+// through a loop with no opening test and no scheduling per node.
 template <bool kLeafRuns>
 __global__ void __launch_bounds__(kWB) k_walk_fp32(Ctx c, int total)
 {
@@ -188,24 +214,23 @@ __global__ void __launch_bounds__(kWB) k_walk_fp32(Ctx c, int total)
   const unsigned full = 0xffffffffu;
   Target t;
   load_target<true>(c, blockIdx.x * kWB + threadIdx.x, total, t);
-  double pot_d = (double)__fdiv_rn(t.mself, P.eps);  // cancels the self term
-  float pot_f = 0.f;
+  PotAcc acc;
   const float theta2 = P.theta2;
-  const float hf = (float)P.h, hinvf = (float)P.h_inv;
+  const float hf = (float)P.h, hinvf = (float)P.h_inv, h2f = hf * hf;
   const double th2d = (double)P.theta2;
   int ninter = 0;
-  unsigned reduces = 0;
+  unsigned steps = 0;
 
   int cur = __reduce_min_sync(full, t.nxt);
   float4 na = make_float4(0.f, 0.f, 0.f, 0.f);
   int2 nm = make_int2(0, 0);
   if (cur != kDone) {
-    na = c.nd_rel[cur];
-    nm = c.nd_meta[cur];
+    load_node(c.nd, cur, na, nm);
   }
   while (cur != kDone) {
-    const float4 pa = c.nd_rel[cur + 1];  // speculative; a spare slot follows the last node
-    const int2 pmeta = c.nd_meta[cur + 1];
+    float4 pa;  // speculative; a spare slot follows the last node
+    int2 pmeta;
+    load_node(c.nd, cur + 1, pa, pmeta);
     const float l2 = __int_as_float(nm.x & 0x7fffffff);
     const bool bottom = kLeafRuns && nm.x < 0;
     const int sk = nm.y;
@@ -220,32 +245,34 @@ __global__ void __launch_bounds__(kWB) k_walk_fp32(Ctx c, int total)
       } else {
         t.nxt = (unsigned)(sk - cur - 1) < (unsigned)(t.end - cur - 1) ? sk : kDone;
         ninter++;
-        interact_fp32(na, r2, pot_f, hf, hinvf);
+        interact(na, r2, acc.f, hf, h2f, hinvf);
       }
     }
-    if (kLeafRuns && __any_sync(full, run)) {
-      // children cur+1 .. sk-1 are particles: stream them
-      const int last = min(sk, t.end);
+    const unsigned runners = kLeafRuns ? __ballot_sync(full, run) : 0u;
+    if (runners) {
+      // children cur+1 .. sk-1 are particles: stream them (every runner is at
+      // cur, in one tree, so the bound is the same for all of them)
+      const int last = __shfl_sync(full, min(sk, t.end), __ffs(runners) - 1);
       int j = cur + 1;
       for (; j + 1 < last; j += 2) {
-        const float4 a0 = c.nd_rel[j], a1 = c.nd_rel[j + 1];
+        const float4 a0 = c.nd[j].p, a1 = c.nd[j + 1].p;
         if (run) {
-          interact_fp32(a0, dist2(a0, t.q), pot_f, hf, hinvf);
-          interact_fp32(a1, dist2(a1, t.q), pot_f, hf, hinvf);
+          interact(a0, dist2(a0, t.q), acc.f, hf, h2f, hinvf);
+          interact(a1, dist2(a1, t.q), acc.f, hf, h2f, hinvf);
         }
       }
       if (j < last) {
-        const float4 a0 = c.nd_rel[j];
-        if (run) interact_fp32(a0, dist2(a0, t.q), pot_f, hf, hinvf);
+        const float4 a0 = c.nd[j].p;
+        if (run) interact(a0, dist2(a0, t.q), acc.f, hf, h2f, hinvf);
       }
       if (run) {
         ninter += last - cur - 1;
         t.nxt = (unsigned)(sk - cur - 1) < (unsigned)(t.end - cur - 1) ? sk : kDone;
       }
+      acc.flush();
       cur = __reduce_min_sync(full, t.nxt);
       if (cur != kDone) {
-        na = c.nd_rel[cur];
-        nm = c.nd_meta[cur];
+        load_node(c.nd, cur, na, nm);
       }
     } else if (__any_sync(full, t.nxt == cur + 1)) {
       cur = cur + 1;
@@ -253,18 +280,70 @@ __global__ void __launch_bounds__(kWB) k_walk_fp32(Ctx c, int total)
       nm = pmeta;
     } else {
       cur = __reduce_min_sync(full, t.nxt);
-      if ((++reduces & 7u) == 0u) {
-        pot_d += (double)pot_f;
-        pot_f = 0.f;
-      }
       if (cur != kDone) {
-        na = c.nd_rel[cur];
-        nm = c.nd_meta[cur];
+        load_node(c.nd, cur, na, nm);
       }
     }
+    if ((++steps & 7u) == 0u) acc.flush();
   }
-  finish_target(c, t, dadd(pot_d, (double)pot_f));
+  finish_target(c, t, acc.total((double)__fdiv_rn(t.mself, P.eps)));  // + cancels the self term
   count_interactions(c, t.s, ninter);
+}
+
+// The reference's opening decision in double, for a target whose float test
+// fell within 1e-5 of the threshold.  Not inlined: the compiler would
+// otherwise evaluate the double arithmetic on every step and select.
+__device__ __noinline__ bool exact_open(float4 na, const float q[3], float l2, double th2d)
+{
+  const double ex = dsub((double)na.x, (double)q[0]);
+  const double ey = dsub((double)na.y, (double)q[1]);
+  const double ez = dsub((double)na.z, (double)q[2]);
+  const double er2 = dadd(dadd(dmul(ex, ex), dmul(ey, ey)), dmul(ez, ez));
+  return (double)l2 > dmul(er2, th2d);
+}
+
+// FP32 walk, lane schedule: the opening test is two compares against
+// per-cell thresholds precomputed from len^2/theta^2 (the reference's double
+// test decides the rare cases in between), every interaction goes straight
+// into a compensated float sum, and the walk ends when the index leaves the
+// tree (skip pointers that leave it are kDone).  The index strictly grows,
+// so the loop ends even on a malformed tree.
+template <int kB>
+__global__ void __launch_bounds__(kB) k_walk_fp32_lean(Ctx c, int total)
+{
+  const DevParams &P = c.P;
+  Target t;
+  load_target<true>(c, blockIdx.x * kB + threadIdx.x, total, t);
+  const float hf = (float)P.h, hinvf = (float)P.h_inv, h2f = hf * hf;
+  const double th2d = (double)P.theta2;
+  float hi = 0.f, comp = 0.f;  // Kahan sum
+  int iters = 0, opens = 0;
+  int cur = t.nxt;
+  const int end = t.end;
+  while (cur < end) {
+    float4 na;
+    int4 nm;
+    load_node(c.nd, cur, na, nm);
+    const float r2 = dist2(na, t.q);
+    const float lo = __int_as_float(nm.z), up = __int_as_float(nm.w);
+    bool open = r2 < lo;
+    if (r2 >= lo && r2 <= up) open = exact_open(na, t.q, __int_as_float(nm.x & 0x7fffffff), th2d);
+    const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
+    const float mass = fabsf(na.w);
+    float contrib = -mass * rinv;
+    if (r2 < h2f) contrib = softened_fp32(mass, r2, rinv, hf, hinvf);
+    contrib = open ? 0.f : contrib;
+    const float y = __fsub_rn(contrib, comp);
+    const float s = __fadd_rn(hi, y);
+    comp = __fsub_rn(__fsub_rn(s, hi), y);
+    hi = s;
+    iters++;
+    opens += open ? 1 : 0;
+    cur = open ? cur + 1 : max(nm.y, cur + 1);
+  }
+  const double base = (double)__fdiv_rn(t.mself, P.eps);  // cancels the self term
+  finish_target(c, t, dadd(dadd(base, (double)hi), -(double)comp));
+  count_interactions(c, t.s, iters - opens);
 }
 
 // FP64: the reference's arithmetic, operation by operation.
@@ -280,7 +359,7 @@ __global__ void __launch_bounds__(kWB) k_walk_fp64(Ctx c, int total)
   int cur = __reduce_min_sync(full, t.nxt);
   while (cur != kDone) {
     const float4 na = c.nd_abs[cur];
-    const int2 nm = c.nd_meta[cur];
+    const int2 nm = make_int2(c.nd[cur].m.x, c.nd[cur].m.y);
     if (t.nxt == cur) {
       double dx = dsub((double)na.x, (double)t.q[0]);
       double dy = dsub((double)na.y, (double)t.q[1]);
@@ -350,8 +429,9 @@ __global__ void __launch_bounds__(kWB) k_grad_walk(Ctx c, int total)
   unsigned reduces = 0;
   int cur = __reduce_min_sync(full, t.nxt);
   while (cur != kDone) {
-    const float4 na = c.nd_rel[cur];
-    const int2 nm = c.nd_meta[cur];
+    float4 na;
+    int2 nm;
+    load_node(c.nd, cur, na, nm);
     if (t.nxt == cur) {
       const float dx = na.x - t.q[0], dy = na.y - t.q[1], dz = na.z - t.q[2];
       const float r2 = dx * dx + dy * dy + dz * dz;
@@ -362,6 +442,7 @@ __global__ void __launch_bounds__(kWB) k_grad_walk(Ctx c, int total)
         t.nxt = (unsigned)(sk - cur - 1) < (unsigned)(t.end - cur - 1) ? sk : kDone;
         const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
         const float r = r2 * rinv;
+        na.w = fabsf(na.w);  // cells carry their mass with the sign bit set
         float w;  // gradient weight: accel += m * w * dx
         if (r >= hf) {
           pot_f -= na.w * rinv;
@@ -426,10 +507,16 @@ void launch_walk(Ctx &c, const PassPlan &pl)
   const unsigned blocks = (n + kWB - 1) / kWB;
   if (c.P.precision == HBTU_PRECISION_FP64)
     k_walk_fp64<<<blocks, kWB, 0, c.st>>>(c, n);
-  else if (c.opt_leaf_runs)
+  else if (c.opt_schedule == 1 && c.opt_leaf_runs)
     k_walk_fp32<true><<<blocks, kWB, 0, c.st>>>(c, n);
-  else
+  else if (c.opt_schedule == 1)
     k_walk_fp32<false><<<blocks, kWB, 0, c.st>>>(c, n);
+  else if (n >= 152 * 4 * 512)  // blocks of neighbouring targets share an SM's L1
+    k_walk_fp32_lean<512><<<(n + 511) / 512, 512, 0, c.st>>>(c, n);
+  else if (n >= 152 * 4 * 256)
+    k_walk_fp32_lean<256><<<(n + 255) / 256, 256, 0, c.st>>>(c, n);
+  else
+    k_walk_fp32_lean<128><<<(n + 127) / 128, 128, 0, c.st>>>(c, n);
   HBTU_LAUNCHED();
 }
 

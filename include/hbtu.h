@@ -200,8 +200,11 @@ hbtu_status hbtu_get_stats(const hbtu_handle *h, hbtu_stats *out);
 hbtu_status hbtu_reset_stats(hbtu_handle *h);
 
 /* Tuning options of a handle (results do not depend on them):
- *   "walk_leaf_runs"  1 (default) or 0: the FP32 walk streams the particles of
- *                     a cell whose children are all particles. */
+ *   "walk_schedule"   how the FP32 walk visits nodes: 0 (default) every
+ *                     lane walks its own target; 1 a warp visits the smallest
+ *                     node index any of its targets waits at (broadcast loads).
+ *   "walk_leaf_runs"  1 (default) or 0: with walk_schedule 1, stream the
+ *                     particles of a cell whose children are all particles. */
 hbtu_status hbtu_set_option(hbtu_handle *h, const char *name, int64_t value);
 hbtu_status hbtu_get_option(const hbtu_handle *h, const char *name, int64_t *value);
 
