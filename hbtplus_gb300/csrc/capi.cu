@@ -84,12 +84,11 @@ static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
   c.sb.hi_b = cv.take<unsigned>(N);
   c.sb.val_a = cv.take<int>(N);
   c.sb.val_b = cv.take<int>(N);
-  const size_t ncount = sort_count_entries(N);
-  c.sb.counts = nullptr;
-  c.sb.counts64 = cv.take<long long>(ncount);
-  const long long scan_n = std::max<long long>(N + 1, (long long)ncount);
-  c.scan_tmp = cv.take<char>(scan_tmp_bytes(scan_n));
-  c.sb.scan_tmp = c.scan_tmp;
+  c.sb.error = c.plan ? &c.plan->error : nullptr;
+  c.sb.os_status = cv.take<unsigned>(sort_status_words(N));
+  c.sb.os_ghist = cv.take<unsigned>(16 * 256);
+  c.sb.os_goff = cv.take<unsigned>(16 * 256);
+  c.scan_tmp = cv.take<char>(scan_tmp_bytes(N + 1));
   c.childL = cv.take<int>(N);
   c.childR = cv.take<int>(N);
   c.parentI = cv.take<int>(N);
@@ -100,9 +99,13 @@ static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
   c.iscell = cv.take<int>(N);
   c.cidx = cv.take<int>(N);
   c.cskip = cv.take<int>(N);
+  c.cdepth = cv.take<int>(N);
   c.pcell = cv.take<int>(N);
-  c.pending = cv.take<int>(N);
   c.pending0 = cv.take<int>(N);
+  c.cslot = cv.take<int>(8 * N);
+  c.cell_list = cv.take<int>(N);
+  c.lvl = cv.take<int>(96);
+  c.pending = cv.take<int>(N);
   c.mask = cv.take<unsigned long long>(N);
   c.X = cv.take<long long>(N + 1);
   // one spare slot: the walk prefetches node cur+1 speculatively
@@ -262,6 +265,7 @@ hbtu_status setup_call(hbtu_handle *h, const hbtu_particles *p, long long S, con
                               c.st));
     // the staging copies above read host memory that lives until the call returns
   }
+  HBTU_CUDA(cudaMemsetAsync(c.plan, 0, sizeof(PassPlan), c.st));
   if (N > 0) launch_init(c, pos, vel, mass, id);
   HBTU_CUDA(cudaStreamSynchronize(c.st));  // segs/segoff are host temporaries
   return HBTU_OK;
@@ -347,6 +351,7 @@ void read_plan(Ctx &c)
 {
   HBTU_CUDA(cudaMemcpyAsync(c.plan_host, c.plan, sizeof(PassPlan), cudaMemcpyDeviceToHost, c.st));
   HBTU_CUDA(cudaStreamSynchronize(c.st));
+  if (c.plan_host->error) throw CudaError(cudaErrorLaunchTimeout, "radix sort look-back", __FILE__, __LINE__);
 }
 
 // One pass's tree and energies for every active subhalo.
@@ -515,7 +520,7 @@ hbtu_status hbtu_set_option(hbtu_handle *h, const char *name, int64_t value)
     return HBTU_OK;
   }
   if (n == "walk_schedule") {
-    if (value != 0 && value != 1) return fail(h, HBTU_ERR_INVALID_ARGUMENT, "walk_schedule: 0 or 1");
+    if (value < 0 || value > 4) return fail(h, HBTU_ERR_INVALID_ARGUMENT, "walk_schedule: 0 to 4");
     h->opt_schedule = value;
     return HBTU_OK;
   }

@@ -132,7 +132,9 @@ struct Ctx {
   SortBuffers sb;
   // tree construction
   int *childL, *childR, *parentI, *parentL, *rfirst, *rlast, *dnode;
-  int *iscell, *cidx, *cskip, *pcell, *pending, *pending0;
+  int *iscell, *cidx, *cskip, *cdepth, *pcell, *pending, *pending0;  // pending: child cells
+  int *cslot;  // 8 per cell: node index of the child in each octant, -1 if none
+  int *cell_list, *lvl;  // cells grouped by octal depth; per-depth counts, starts, cursors
   unsigned long long *mask;
   long long *X;
   // nodes (2 per tree particle)

@@ -68,6 +68,10 @@ struct SegState {
   int refine;           // RefineBindingEnergyOrder pending (sampling, converged)
   int levels;
   double center[3], len;
+  // octal keys in 64-bit fixed point (units of 2^-kscale) when every centre
+  // of the subdivision is exact in double (kfast), see k_cube
+  long long kc[3], kinc;
+  int kscale, kfast;
   float fc[3];  // frame centre of the relative coordinates
   // frames (HBTxyz floats)
   float ref_pos[3], ref_vel[3], old_pos[3], old_vel[3];
@@ -88,6 +92,7 @@ struct PassPlan {
   int nsort_total;  // elements of the unbound-part sort
   int nchunks_bound;
   int nrefine;
+  int error;             // a sort's look-back wait ran out
   long long inter_done;  // walk interactions summed so far, all subhaloes
 };
 
@@ -123,11 +128,11 @@ struct SortBuffers {
   unsigned long long *lo_a, *lo_b;
   unsigned *hi_a, *hi_b;
   int *val_a, *val_b;
-  unsigned *counts;  // 256 * max blocks
-  long long *counts64;
-  void *scan_tmp;
+  unsigned *os_status;         // sort_status_words(N): per-tile look-back words + tile counter
+  unsigned *os_ghist, *os_goff;  // 16 x 256 digit counts and offsets
+  int *error;                  // set when a look-back wait ran out (in the pass plan)
 };
-size_t sort_count_entries(long long n);
+size_t sort_status_words(long long n);
 // passes: list of (word, shift) pairs; word 0 = lo, 1 = hi; LSD order.
 void radix_sort(SortBuffers &b, long long n, const int *words, const int *shifts, int npasses,
                 cudaStream_t st);

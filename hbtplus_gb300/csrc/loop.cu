@@ -54,7 +54,15 @@ __device__ void plan_scan4(int S, int (*getter)(const Ctx &, int, int *), const 
   const int per = (S + kPlanThreads - 1) / kPlanThreads;
   const int b = threadIdx.x * per, e = min(S, b + per);
   int loc[4] = {0, 0, 0, 0}, v[4];
-  for (int s = b; s < e; s++) {
+  constexpr int kKeep = 4;  // segments per thread whose counters stay in registers
+  int kept[kKeep][4];
+#pragma unroll
+  for (int q = 0; q < kKeep; q++)
+    if (b + q < e) {
+      getter(c, b + q, kept[q]);
+      for (int k = 0; k < 4; k++) loc[k] += kept[q][k];
+    }
+  for (int s = b + kKeep; s < e; s++) {
     getter(c, s, v);
     for (int k = 0; k < 4; k++) loc[k] += v[k];
   }
@@ -84,7 +92,14 @@ __device__ void plan_scan4(int S, int (*getter)(const Ctx &, int, int *), const 
   int run[4];
   for (int k = 0; k < 4; k++) run[k] = (w > 0 ? wsum[k][w - 1] : 0) + inc[k] - loc[k];
   int *outs[4] = {out0, out1, out2, out3};
-  for (int s = b; s < e; s++) {
+#pragma unroll
+  for (int q = 0; q < kKeep; q++)
+    if (b + q < e)
+      for (int k = 0; k < 4; k++) {
+        if (outs[k]) outs[k][b + q] = run[k];
+        run[k] += kept[q][k];
+      }
+  for (int s = b + kKeep; s < e; s++) {
     getter(c, s, v);
     for (int k = 0; k < 4; k++) {
       if (outs[k]) outs[k][s] = run[k];
@@ -180,8 +195,13 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode)
       cnt += c.seg[s].status == SEG_ACTIVE;
       it += (unsigned long long)c.seg[s].interactions;
     }
-    atomicAdd(&nact, cnt);
-    atomicAdd(&inter, it);
+    // warp sums first: one shared atomic per warp, not per thread
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    for (int o = 16; o > 0; o >>= 1) it += __shfl_xor_sync(0xffffffffu, it, o);
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(&nact, cnt);
+      atomicAdd(&inter, it);
+    }
     __syncthreads();
     if (threadIdx.x == 0) c.plan->inter_done = (long long)inter;
     plan_scan4(c.S, get_pass, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
@@ -383,12 +403,22 @@ __global__ void __launch_bounds__(kLB) k_avg_chunks(Ctx c)
 // ---------------------------------------------------------------- control
 __global__ void k_control(Ctx c, int max_passes)
 {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per subhalo: lanes 0..6 add the 7 chunk sums in chunk order
+  // (each an independent chain), lane 0 then takes the decisions
+  const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (s >= c.S) return;
   SegState &sg = c.seg[s];
   if (sg.status != SEG_ACTIVE) return;
   const DevParams &P = c.P;
   const int nb = c.part_info[8 * s + 7];
+  double part = 0.;
+  if (nb > 1 && lane < 7)
+    for (int b = c.bchunk_base[s]; b < c.bchunk_base[s + 1]; b++)
+      part += c.chunk_sums[(size_t)b * kSums + lane];
+  double v[7];
+#pragma unroll
+  for (int k = 0; k < 7; k++) v[k] = __shfl_sync(0xffffffffu, part, k);
+  if (lane != 0) return;
   const int nl = sg.nlast;
   sg.passes++;
   sg.evals += sg.ntgt;
@@ -428,9 +458,6 @@ __global__ void k_control(Ctx c, int max_passes)
     sg.ref_pos[1] = a.y;
     sg.ref_pos[2] = a.z;
   } else if (nb > 1) {
-    double v[7] = {0, 0, 0, 0, 0, 0, 0};
-    for (int b = c.bchunk_base[s]; b < c.bchunk_base[s + 1]; b++)
-      for (int k = 0; k < 7; k++) v[k] += c.chunk_sums[(size_t)b * kSums + k];
     const double msum = v[0];
     sg.mbound = (float)msum;
     for (int j = 0; j < 3; j++) sg.ref_vel[j] = __double2float_rn(ddiv(v[1 + j], msum));
@@ -604,20 +631,33 @@ __global__ void __launch_bounds__(kLB) k_kin_chunks(Ctx c)
     v[5] += (double)m;
     const int t = c.type ? c.type[pid] : 1;
     const bool skip = (nb <= 100 && c.id[pid] == -1) || t < 0 || t > 5;
-    if (!skip) {
-      v[6 + t] += 1.0;
-      v[12 + t] += (double)m;
-    }
+#pragma unroll
+    for (int q = 0; q < 6; q++)
+      if (!skip && q == t) {
+        v[6 + q] += 1.0;
+        v[12 + q] += (double)m;
+      }
   }
   block_sum<18>(v, c.chunk_sums + (size_t)b * kSums);
 }
 
 __global__ void k_final_seg(Ctx c, hbtu_result *res)
 {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per subhalo: lanes 0..17 add the 18 chunk sums in chunk order,
+  // lane 0 then writes the result
+  const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (s >= c.S) return;
   const SegState &sg = c.seg[s];
   const DevParams &P = c.P;
+  const bool summed = sg.status != SEG_TRIVIAL && sg.status != SEG_DISRUPTED;
+  double part = 0.;
+  if (summed && lane < 18)
+    for (int b = c.bchunk_base[s]; b < c.bchunk_base[s + 1]; b++)
+      part += c.chunk_sums[(size_t)b * kSums + lane];
+  double v[18];
+#pragma unroll
+  for (int k = 0; k < 18; k++) v[k] = __shfl_sync(0xffffffffu, part, k);
+  if (lane != 0) return;
   hbtu_result r;
   memset(&r, 0, sizeof(r));
   r.too_few = sg.n < P.minpart;
@@ -669,10 +709,6 @@ __global__ void k_final_seg(Ctx c, hbtu_result *res)
       r.mostbound_vel[1] = u.y;
       r.mostbound_vel[2] = u.z;
     }
-    double v[18];
-    for (int k = 0; k < 18; k++) v[k] = 0.;
-    for (int b = c.bchunk_base[s]; b < c.bchunk_base[s + 1]; b++)
-      for (int k = 0; k < 18; k++) v[k] += c.chunk_sums[(size_t)b * kSums + k];
     if (sg.nbound > 1) {
       const double M = v[5];
       const double E = ddiv(v[0], M);
@@ -795,7 +831,7 @@ void launch_averages_control(Ctx &c, int max_passes)
   const int max_chunks = (c.N + kChunk - 1) / kChunk + c.S;
   k_avg_chunks<<<max_chunks, kLB, 0, c.st>>>(c);
   HBTU_LAUNCHED();
-  k_control<<<nblk(c.S, 128), 128, 0, c.st>>>(c, max_passes);
+  k_control<<<nblk(32ll * c.S, 128), 128, 0, c.st>>>(c, max_passes);
   HBTU_LAUNCHED();
 }
 
@@ -838,7 +874,7 @@ void launch_finalize(Ctx &c, int64_t *order_out, float *energy_out, hbtu_result 
   const int max_chunks = (c.N + kChunk - 1) / kChunk + c.S;
   k_kin_chunks<<<max_chunks, kLB, 0, c.st>>>(c);
   HBTU_LAUNCHED();
-  k_final_seg<<<nblk(c.S, 128), 128, 0, c.st>>>(c, res_dev);
+  k_final_seg<<<nblk(32ll * c.S, 128), 128, 0, c.st>>>(c, res_dev);
   HBTU_LAUNCHED();
   if (c.N > 0) {
     k_final_out<<<nblk(c.N), kLB, 0, c.st>>>(c, order_out, energy_out);

@@ -143,6 +143,7 @@ extern "C" hbtu_status hbtu_unbind_noalloc(const hbtu_params *params, const hbtu
     HBTU_CUDA(cudaMemcpyAsync(c.seg, &g, sizeof(SegState), cudaMemcpyHostToDevice, c.st));
     HBTU_CUDA(cudaMemcpyAsync(c.seg_off, segoff, sizeof(segoff), cudaMemcpyHostToDevice, c.st));
     HBTU_CUDA(cudaMemcpyAsync(c.seg_order, order, sizeof(order), cudaMemcpyHostToDevice, c.st));
+    HBTU_CUDA(cudaMemsetAsync(c.plan, 0, sizeof(PassPlan), c.st));
     if (n > 0) launch_init(c, p->pos, p->vel, p->mass, (const long long *)p->id);
     HBTU_CUDA(cudaStreamSynchronize(c.st));  // the stack copies above are consumed
     const int max_passes = params->max_passes > 0 ? params->max_passes : 10000;

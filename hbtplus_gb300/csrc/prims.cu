@@ -2,9 +2,10 @@
 // build (Morton-key sort) and by the energy-ordering sorts of the unbinding
 // loop (src/subhalo_unbind.cpp:382, :405).  Both are HBM-bound integer work:
 // one read and one write of each record per pass, tiles of 2048 records per
-// 256-thread block.
+// 256-thread block; up to 4096 records sort in one block in shared memory.
 #include "hbtu_internal.h"
 
+#include <algorithm>
 #include <cstdio>
 #include <utility>
 
@@ -89,51 +90,240 @@ __device__ __forceinline__ unsigned rs_digit(unsigned hi, unsigned long long lo,
   return word ? (hi >> shift) & 255u : (unsigned)(lo >> shift) & 255u;
 }
 
-__global__ void __launch_bounds__(kBlock) k_rs_hist(const unsigned *hi,
-                                                    const unsigned long long *lo, long long n,
-                                                    int word, int shift, long long *counts,
-                                                    int nblocks)
+// Every pass of a sort of at most kSmallN records in one block, the records
+// held in shared memory between passes: the same stable histogram /
+// scan / ranked-scatter steps as the multi-block passes, without a launch
+// per step.
+constexpr int kSmallN = 2 * kTile;  // 4096 records, 128 KB of shared memory
+
+struct SmallSortPasses {
+  int words[16], shifts[16], n;
+};
+
+__global__ void __launch_bounds__(kBlock) k_rs_small(unsigned *hi_g, unsigned long long *lo_g,
+                                                     int *val_g, int n, SmallSortPasses ps)
 {
+  extern __shared__ __align__(16) unsigned char smem[];
+  // two buffers of each field: field(b) + b * kSmallN
+  unsigned long long *const lo0 = (unsigned long long *)smem;
+  unsigned *const hi0 = (unsigned *)(lo0 + 2 * kSmallN);
+  int *const val0 = (int *)(hi0 + 2 * kSmallN);
   __shared__ unsigned hist[256];
-  hist[threadIdx.x] = 0;
-  __syncthreads();
-  const long long tile = (long long)blockIdx.x * kTile;
-#pragma unroll
-  for (int r = 0; r < kItems; r++) {
-    long long e = tile + r * kBlock + threadIdx.x;
-    if (e < n) atomicAdd(&hist[rs_digit(word ? hi[e] : 0u, word ? 0ull : lo[e], word, shift)], 1u);
+  __shared__ unsigned wcnt[kBlock / 32][256];
+  __shared__ unsigned run_base[256];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int e = tid; e < n; e += kBlock) {
+    lo0[e] = lo_g[e];
+    hi0[e] = hi_g[e];
+    val0[e] = val_g[e];
   }
-  __syncthreads();
-  counts[(long long)threadIdx.x * nblocks + blockIdx.x] = hist[threadIdx.x];
+  const unsigned lt = (1u << lane) - 1u;
+  int cur = 0;
+  for (int p = 0; p < ps.n; p++) {
+    const int word = ps.words[p], shift = ps.shifts[p];
+    hist[tid] = 0;
+    run_base[tid] = 0;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; w++) wcnt[w][tid] = 0;
+    __syncthreads();
+    for (int e = tid; e < n; e += kBlock)
+      atomicAdd(&hist[rs_digit(word ? hi0[cur * kSmallN + e] : 0u, word ? 0ull : lo0[cur * kSmallN + e], word, shift)], 1u);
+    __syncthreads();
+    {  // exclusive scan of the 256 digit counts (thread tid owns digit tid)
+      const unsigned v = hist[tid];
+      unsigned x = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      __shared__ unsigned wsum[kBlock / 32];
+      if (lane == 31) wsum[warp] = x;
+      __syncthreads();
+      unsigned before = 0;
+      for (int w = 0; w < warp; w++) before += wsum[w];
+      __syncthreads();
+      hist[tid] = before + x - v;  // start of digit tid
+    }
+    __syncthreads();
+    for (int r = 0; r * kBlock < n; r++) {
+      const int e = r * kBlock + tid;
+      const bool valid = e < n;
+      unsigned h = 0, d = 256u + lane;  // unique sentinel for invalid lanes
+      unsigned long long l = 0;
+      int v = 0;
+      if (valid) {
+        h = hi0[cur * kSmallN + e];
+        l = lo0[cur * kSmallN + e];
+        v = val0[cur * kSmallN + e];
+        d = rs_digit(h, l, word, shift);
+      }
+      const unsigned mask = __match_any_sync(0xffffffffu, d);
+      const unsigned rank = __popc(mask & lt);
+      if (valid && rank == 0) wcnt[warp][d] = __popc(mask);
+      __syncthreads();
+      {
+        unsigned run = run_base[tid];
+#pragma unroll
+        for (int w = 0; w < kBlock / 32; w++) {
+          const unsigned t = wcnt[w][tid];
+          wcnt[w][tid] = run;
+          run += t;
+        }
+        run_base[tid] = run;
+      }
+      __syncthreads();
+      if (valid) {
+        const unsigned dst = hist[d] + wcnt[warp][d] + rank;
+        hi0[(cur ^ 1) * kSmallN + dst] = h;
+        lo0[(cur ^ 1) * kSmallN + dst] = l;
+        val0[(cur ^ 1) * kSmallN + dst] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int w = 0; w < kBlock / 32; w++) wcnt[w][tid] = 0;
+      __syncthreads();
+    }
+    cur ^= 1;
+  }
+  for (int e = tid; e < n; e += kBlock) {
+    lo_g[e] = lo0[cur * kSmallN + e];
+    hi_g[e] = hi0[cur * kSmallN + e];
+    val_g[e] = val0[cur * kSmallN + e];
+  }
 }
 
-__global__ void __launch_bounds__(kBlock) k_rs_scatter(
+constexpr size_t kSmallSortSmem = (size_t)kSmallN * 2 * (8 + 4 + 4);
+
+// ---------------------------------------------------------------- onesweep
+// Larger sorts: one kernel per digit (Adinets & Merrill 2022, "Onesweep").
+// The global offset of every digit value is known up front (one histogram
+// pass over all digits); each tile then finds how many earlier elements
+// share its digit values by decoupled look-back over the tiles before it
+// (tile indices come from an atomic counter, so a tile only waits on tiles
+// that have started), and scatters with the same stable ranks as above.
+// Status words: bits 30-31 flag (1 = tile count, 2 = inclusive prefix),
+// bits 0-29 the count.  Every wait is bounded; a wait that runs out sets
+// *err and the pass continues (results are then wrong and the call fails).
+constexpr unsigned kFlagAgg = 1u << 30, kFlagPre = 2u << 30, kCountMask = (1u << 30) - 1u;
+constexpr int kMaxPasses = 16;
+constexpr long long kSpinLimit = 1ll << 24;
+
+struct Passes {
+  int words[kMaxPasses], shifts[kMaxPasses], n;
+};
+
+__global__ void __launch_bounds__(kBlock) k_os_hist(const unsigned *hi,
+                                                    const unsigned long long *lo, long long n,
+                                                    Passes ps, unsigned *ghist)
+{
+  __shared__ unsigned h[kMaxPasses][256];
+  for (int p = 0; p < ps.n; p++) h[p][threadIdx.x] = 0;
+  __syncthreads();
+  for (long long e = (long long)blockIdx.x * kBlock + threadIdx.x; e < n;
+       e += (long long)gridDim.x * kBlock) {
+    const unsigned hv = hi[e];
+    const unsigned long long lv = lo[e];
+    for (int p = 0; p < ps.n; p++)
+      atomicAdd(&h[p][rs_digit(hv, lv, ps.words[p], ps.shifts[p])], 1u);
+  }
+  __syncthreads();
+  for (int p = 0; p < ps.n; p++)
+    if (h[p][threadIdx.x]) atomicAdd(&ghist[p * 256 + threadIdx.x], h[p][threadIdx.x]);
+}
+
+// Exclusive scan of each digit's 256 counts (one block, thread = digit value).
+__global__ void __launch_bounds__(kBlock) k_os_offsets(const unsigned *ghist, int npasses,
+                                                       unsigned *goff)
+{
+  __shared__ unsigned wsum[kBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int p = 0; p < npasses; p++) {
+    const unsigned v = ghist[p * 256 + threadIdx.x];
+    unsigned x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    unsigned before = 0;
+    for (int w = 0; w < warp; w++) before += wsum[w];
+    goff[p * 256 + threadIdx.x] = before + x - v;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_os_pass(
     const unsigned *hi_in, const unsigned long long *lo_in, const int *val_in, unsigned *hi_out,
     unsigned long long *lo_out, int *val_out, long long n, int word, int shift,
-    const long long *offsets, int nblocks)
+    const unsigned *goff, unsigned *status, int *tile_counter, int *err)
 {
   __shared__ unsigned wcnt[kBlock / 32][256];
   __shared__ unsigned run_base[256];
-  __shared__ long long goff[256];
+  __shared__ unsigned hist[256];
+  __shared__ unsigned base[256];
+  __shared__ int tile_s;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  goff[tid] = offsets[(long long)tid * nblocks + blockIdx.x];
+  if (tid == 0) tile_s = atomicAdd(tile_counter, 1);
+  hist[tid] = 0;
   run_base[tid] = 0;
 #pragma unroll
   for (int w = 0; w < kBlock / 32; w++) wcnt[w][tid] = 0;
   __syncthreads();
-  const unsigned lt = (1u << lane) - 1u;
-  const long long tile = (long long)blockIdx.x * kTile;
+  const int tile = tile_s;
+  const long long t0 = (long long)tile * kTile;
+  // this tile's digits, kept for the scatter
+  unsigned dg[kItems];
+#pragma unroll
   for (int r = 0; r < kItems; r++) {
-    const long long e = tile + r * kBlock + tid;
+    const long long e = t0 + r * kBlock + tid;
+    dg[r] = 256u;
+    if (e < n) {
+      dg[r] = rs_digit(hi_in[e], lo_in[e], word, shift);
+      atomicAdd(&hist[dg[r]], 1u);
+    }
+  }
+  __syncthreads();
+  // publish this tile's counts, then look back for the earlier tiles' total
+  volatile unsigned *st = status;
+  const unsigned cnt = hist[tid];
+  st[(long long)tile * 256 + tid] = (tile == 0 ? kFlagPre : kFlagAgg) | cnt;
+  unsigned prefix = 0;
+  for (int k = tile - 1; k >= 0;) {
+    const unsigned v = st[(long long)k * 256 + tid];
+    const unsigned flag = v & ~kCountMask;
+    if (flag == 0u) {
+      long long spins = 0;
+      unsigned w = 0;
+      while ((w = st[(long long)k * 256 + tid]) == 0u && ++spins < kSpinLimit) {
+      }
+      if (w == 0u) {  // the earlier tile never published: give up on this pass
+        atomicExch(err, 1);
+        break;
+      }
+      continue;
+    }
+    prefix += v & kCountMask;
+    if (flag == kFlagPre) break;
+    k--;
+  }
+  if (tile > 0) st[(long long)tile * 256 + tid] = kFlagPre | ((prefix + cnt) & kCountMask);
+  base[tid] = goff[tid] + prefix;
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1u;
+  for (int r = 0; r < kItems; r++) {
+    const long long e = t0 + r * kBlock + tid;
     const bool valid = e < n;
-    unsigned h = 0, d = 256u + lane;  // unique sentinel for invalid lanes
+    unsigned h = 0;
     unsigned long long l = 0;
     int v = 0;
+    const unsigned d = valid ? dg[r] : 256u + lane;  // unique sentinel for invalid lanes
     if (valid) {
       h = hi_in[e];
       l = lo_in[e];
       v = val_in[e];
-      d = rs_digit(h, l, word, shift);
     }
     const unsigned mask = __match_any_sync(0xffffffffu, d);
     const unsigned rank = __popc(mask & lt);
@@ -143,7 +333,7 @@ __global__ void __launch_bounds__(kBlock) k_rs_scatter(
       unsigned run = run_base[tid];
 #pragma unroll
       for (int w = 0; w < kBlock / 32; w++) {
-        unsigned t = wcnt[w][tid];
+        const unsigned t = wcnt[w][tid];
         wcnt[w][tid] = run;
         run += t;
       }
@@ -151,7 +341,7 @@ __global__ void __launch_bounds__(kBlock) k_rs_scatter(
     }
     __syncthreads();
     if (valid) {
-      const long long dst = goff[d] + wcnt[warp][d] + rank;
+      const long long dst = (long long)base[d] + wcnt[warp][d] + rank;
       hi_out[dst] = h;
       lo_out[dst] = l;
       val_out[dst] = v;
@@ -194,26 +384,54 @@ void exclusive_scan_i64(const long long *in, long long *out, long long n, void *
   HBTU_LAUNCHED();
 }
 
-size_t sort_count_entries(long long n)
+size_t sort_status_words(long long n)
 {
   long long nb = (n + kTile - 1) / kTile;
   if (nb < 1) nb = 1;
-  return (size_t)nb * 256;
+  return (size_t)nb * 256 + 16;  // + the tile counter
 }
 
 void radix_sort(SortBuffers &b, long long n, const int *words, const int *shifts, int npasses,
                 cudaStream_t st)
 {
   if (n <= 1 || npasses <= 0) return;
-  const int nblocks = (int)((n + kTile - 1) / kTile);
-  const long long ncount = (long long)nblocks * 256;
-  for (int p = 0; p < npasses; p++) {
-    k_rs_hist<<<nblocks, kBlock, 0, st>>>(b.hi_a, b.lo_a, n, words[p], shifts[p], b.counts64,
-                                           nblocks);
+  if (n <= kSmallN && npasses <= 16) {
+    // more than 48 KB of shared memory needs an opt-in (per device, so every time)
+    HBTU_CUDA(cudaFuncSetAttribute(k_rs_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kSmallSortSmem));
+    SmallSortPasses ps;
+    ps.n = npasses;
+    for (int p = 0; p < npasses; p++) {
+      ps.words[p] = words[p];
+      ps.shifts[p] = shifts[p];
+    }
+    k_rs_small<<<1, kBlock, kSmallSortSmem, st>>>(b.hi_a, b.lo_a, b.val_a, (int)n, ps);
     HBTU_LAUNCHED();
-    exclusive_scan_i64(b.counts64, b.counts64, ncount, b.scan_tmp, st);
-    k_rs_scatter<<<nblocks, kBlock, 0, st>>>(b.hi_a, b.lo_a, b.val_a, b.hi_b, b.lo_b, b.val_b, n,
-                                              words[p], shifts[p], b.counts64, nblocks);
+    return;
+  }
+  if (npasses > kMaxPasses)
+    throw CudaError(cudaErrorInvalidValue, "radix sort: too many digit passes", __FILE__, __LINE__);
+  const long long ntiles = (n + kTile - 1) / kTile;
+  Passes ps;
+  ps.n = npasses;
+  for (int p = 0; p < npasses; p++) {
+    ps.words[p] = words[p];
+    ps.shifts[p] = shifts[p];
+  }
+  // global digit counts of every pass, their offsets, then one kernel per pass
+  HBTU_CUDA(cudaMemsetAsync(b.os_ghist, 0, sizeof(unsigned) * 256 * kMaxPasses, st));
+  const unsigned hblocks = (unsigned)std::min<long long>(ntiles, 152 * 4);
+  k_os_hist<<<hblocks, kBlock, 0, st>>>(b.hi_a, b.lo_a, n, ps, b.os_ghist);
+  HBTU_LAUNCHED();
+  k_os_offsets<<<1, kBlock, 0, st>>>(b.os_ghist, npasses, b.os_goff);
+  HBTU_LAUNCHED();
+  for (int p = 0; p < npasses; p++) {
+    HBTU_CUDA(cudaMemsetAsync(b.os_status, 0, sizeof(unsigned) * 256 * ntiles + 64, st));
+    int *tiles = reinterpret_cast<int *>(b.os_status + 256 * ntiles);
+    k_os_pass<<<(unsigned)ntiles, kBlock, 0, st>>>(b.hi_a, b.lo_a, b.val_a, b.hi_b, b.lo_b,
+                                                   b.val_b, n, words[p], shifts[p],
+                                                   b.os_goff + 256 * p, b.os_status, tiles,
+                                                   b.error);
     HBTU_LAUNCHED();
     std::swap(b.hi_a, b.hi_b);
     std::swap(b.lo_a, b.lo_b);

@@ -27,6 +27,7 @@ namespace hbtu {
 namespace {
 
 constexpr int kTB = 256;
+constexpr int kLevelSyncMin = 1 << 16;  // tree particles from which moments go level by level
 
 __global__ void __launch_bounds__(kTB) k_bbox_chunks(Ctx c)
 {
@@ -70,6 +71,64 @@ __global__ void __launch_bounds__(kTB) k_bbox_chunks(Ctx c)
   }
 }
 
+// Fixed-point form of the key computation.  The reference halves the cube in
+// double: centre_k = centre_{k-1} +- len / 2^(k+1).  When the centre, len/4
+// and every later increment are integers in units of 2^-E, and every centre
+// fits in 53 significant bits, none of those double operations rounds, so the
+// same comparisons x > centre_k can be made exactly on 64-bit integers
+// (a tenth of the cost: double runs at 1/64 of the FP32 rate on this GPU).
+__device__ __forceinline__ int ll_tz(long long v) { return v ? __ffsll(v) - 1 : 64; }
+
+__device__ void fixed_point_cube(SegState &sg, int levels)
+{
+  sg.kfast = 0;
+  if (levels <= 0 || !(sg.len > 0.)) return;
+  double M = sg.len;
+  for (int j = 0; j < 3; j++) M = fmax(M, fabs(sg.center[j]) + sg.len);
+  int top;
+  frexp(M, &top);                // M < 2^top
+  const int E = 61 - top;        // |values| < 2^61 in fixed point
+  const double l4 = ldexp(sg.len, E - 2);
+  const double lmin = ldexp(sg.len, E - levels - 1);
+  if (l4 != trunc(l4) || lmin != trunc(lmin) || l4 >= 0x1p62) return;
+  const long long inc = (long long)l4;
+  int g = ll_tz(inc >> (levels - 1));  // trailing zeros of the smallest increment
+  for (int j = 0; j < 3; j++) {
+    const double cj = ldexp(sg.center[j], E);
+    if (cj != trunc(cj) || fabs(cj) >= 0x1p62) return;
+    sg.kc[j] = (long long)cj;
+    g = min(g, ll_tz(sg.kc[j]));
+  }
+  if (top + E - g > 53) return;  // some centre would need more than 53 bits
+  sg.kinc = inc;
+  sg.kscale = E;
+  sg.kfast = 1;
+}
+
+// A float position in units of 2^-E, if exact (else false).
+__device__ __forceinline__ bool float_fixed(float x, int E, long long &X)
+{
+  const unsigned b = __float_as_uint(x);
+  const int ex = (int)((b >> 23) & 255u);
+  if (ex == 0) {  // zero (denormals take the double path)
+    X = 0;
+    return (b & 0x7fffffffu) == 0u;
+  }
+  if (ex == 255) return false;
+  const long long mant = (long long)((b & 0x7fffffu) | 0x800000u);
+  const int sh = ex - 150 + E;  // x = mant * 2^(ex - 150)
+  long long v;
+  if (sh >= 0) {
+    if (sh > 37) return false;  // would pass 2^61
+    v = mant << sh;
+  } else {
+    if (-sh > 24 || (mant & ((1ll << -sh) - 1)) != 0) return false;
+    v = mant >> -sh;
+  }
+  X = (b >> 31) ? -v : v;
+  return true;
+}
+
 // Root cube of each active subhalo (src/oct_tree.tpp:30-51) and its depth of
 // geometric subdivision: the first level whose side is below TreeNodeResolution
 // (the len halving rule of src/gravity_tree.cpp:37-40).
@@ -105,6 +164,7 @@ __global__ void k_cube(Ctx c)
     levels++;
   }
   sg.levels = levels;
+  fixed_point_cube(sg, levels);
   for (int j = 0; j < 3; j++) sg.fc[j] = sg.ref_pos[j];
   atomicMax(&c.plan->max_levels, levels);
 }
@@ -120,9 +180,31 @@ __global__ void __launch_bounds__(kTB) k_keys(Ctx c, int ntotal)
   const int epos = sg.off + sg.t0 + (e - c.tree_base[s]);
   const float4 a = c.pm[c.epid[epos]];
   const float x[3] = {a.x, a.y, a.z};
+  unsigned long long key = 0;
+  long long X[3];
+  if (sg.kfast && float_fixed(x[0], sg.kscale, X[0]) && float_fixed(x[1], sg.kscale, X[1]) &&
+      float_fixed(x[2], sg.kscale, X[2])) {
+    long long cen[3] = {sg.kc[0], sg.kc[1], sg.kc[2]};
+    long long inc = sg.kinc;
+    for (int k = 0; k < sg.levels; k++) {
+      unsigned d = 0;
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const bool gt = X[j] > cen[j];
+        cen[j] += gt ? inc : -inc;
+        d |= (unsigned)gt << j;
+      }
+      inc >>= 1;
+      key = (key << 3) | d;
+    }
+    if (sg.levels > 0) key <<= (64 - 3 * sg.levels);
+    c.sb.lo_a[e] = key;
+    c.sb.hi_a[e] = (unsigned)s;
+    c.sb.val_a[e] = epos;
+    return;
+  }
   double cen[3] = {sg.center[0], sg.center[1], sg.center[2]};
   double lenhalf = dmul(0.5, sg.len);
-  unsigned long long key = 0;
   for (int k = 0; k < sg.levels; k++) {
     lenhalf = dmul(lenhalf, 0.5);
     unsigned d = 0;
@@ -199,6 +281,12 @@ __global__ void __launch_bounds__(kTB) k_karras(Ctx c, int ntotal)
 }
 
 __device__ __forceinline__ int oct_depth(int dn, int levels) { return min(dn / 3, levels); }
+
+// Octant digit at depth k (1-based) of a left-aligned key.
+__device__ __forceinline__ int octant_at(unsigned long long key, int k)
+{
+  return (int)(key >> (64 - 3 * k)) & 7;
+}
 
 // An internal node is an octree cell when its octal depth exceeds its
 // parent's (the root always is).  Record depth bits per first key.
@@ -281,13 +369,25 @@ __global__ void __launch_bounds__(kTB) k_leaves(Ctx c, int ntotal)
   c.nd[nb + idx].p = make_rel(a, sg.fc, c.P);
   c.nd[nb + idx].m = particle_meta(idx + 1 < nnodes ? nb + idx + 1 : kDone);
   if (j == 0) sg.nnodes = nnodes;
+  // the octant slot in the lowest cell holding this particle (none in a bucket)
+  int p = c.parentL[e];
+  for (int guard = 0; p >= 0 && !c.iscell[p] && guard < 256; guard++) p = c.parentI[p];
+  if (p >= 0 && c.iscell[p]) {
+    const int odp = oct_depth(c.dnode[p], sg.levels);
+    if (odp < sg.levels) c.cslot[8 * p + octant_at(c.sb.lo_a[e], odp + 1)] = nb + idx;
+  }
 }
 
-// Cells: preorder index, skip pointer, side (len*len in float), parent cell.
+// Cells: preorder index, skip pointer, side (len*len in float), octal depth,
+// and a count of child cells on the parent.
 __global__ void __launch_bounds__(kTB) k_cellnodes(Ctx c, int ntotal)
 {
   const int e = blockIdx.x * kTB + threadIdx.x;
-  if (e >= ntotal || !c.iscell[e]) return;
+  if (e >= ntotal) return;
+  if (!c.iscell[e]) {
+    c.cdepth[e] = -1;
+    return;
+  }
   const int s = c.sb.hi_a[e];
   const SegState &sg = c.seg[s];
   const int base = c.tree_base[s];
@@ -307,38 +407,60 @@ __global__ void __launch_bounds__(kTB) k_cellnodes(Ctx c, int ntotal)
   c.nd[nb + idx].m = cell_meta(fmul(lf, lf), hi + 1 < n ? nb + skip : kDone, c.P);
   c.cidx[e] = nb + idx;
   c.cskip[e] = nb + skip;
+  c.cdepth[e] = od;
   int p = c.parentI[e];
   for (int guard = 0; p >= 0 && !c.iscell[p] && guard < 256; guard++) p = c.parentI[p];
   if (p >= 0 && !c.iscell[p]) p = -1;  // malformed tree: never climb past it
   c.pcell[e] = p;
-  if (p >= 0) atomicAdd(&c.pending[p], 1);
+  if (p >= 0) {
+    atomicAdd(&c.pending[p], 1);
+    const int odp = oct_depth(c.dnode[p], sg.levels);
+    c.cslot[8 * p + octant_at(c.sb.lo_a[base + lo], odp + 1)] = nb + idx;
+  }
 }
 
 // Bottom-up moments: a cell is summed once all its child cells are, by the
-// thread that finished the last child (atomic countdown, no waiting).
+// thread that finished the last child (atomic countdown, no waiting): mass
+// and centre of mass over the children in octant order, in double, rounded
+// to float per cell as the reference does.  The children are read from the
+// cell's eight octant slots with independent loads; a bucket cell (particles
+// sharing the whole key) walks its children by skip pointers.  A cell
+// without child cells is marked for the walk's leaf runs (sign bit of
+// len*len).
+__device__ __forceinline__ void add_child(const Ctx &c, int k, double &m, double &cx, double &cy,
+                                          double &cz)
+{
+  const float4 a = __ldcg(&c.nd_abs[k]);
+  const double w = (double)a.w;
+  m = dadd(m, w);
+  cx = dadd(cx, dmul((double)a.x, w));
+  cy = dadd(cy, dmul((double)a.y, w));
+  cz = dadd(cz, dmul((double)a.z, w));
+}
+
 __global__ void __launch_bounds__(kTB) k_moments(Ctx c, int ntotal)
 {
   int e = blockIdx.x * kTB + threadIdx.x;
   if (e >= ntotal || !c.iscell[e] || c.pending0[e] != 0) return;
-  const int s = c.sb.hi_a[e];
-  const SegState &sg = c.seg[s];
-  {
-    // a cell without child cells: mark it for the walk's leaf runs (sign bit of len*len)
-    int *meta = &c.nd[c.cidx[e]].m.x;
-    *meta = *meta | (int)0x80000000;
-  }
+  c.nd[c.cidx[e]].m.x |= (int)0x80000000;
   for (int level = 0; level <= 2 * kMaxLevels + 2; level++) {
+    const int s = c.sb.hi_a[e];
+    const SegState &sg = c.seg[s];
     const int idx = c.cidx[e], end = c.cskip[e];
     double m = 0., cx = 0., cy = 0., cz = 0.;
-    for (int k = idx + 1; k < end;) {
-      const float4 a = __ldcg(&c.nd_abs[k]);
-      const double w = (double)a.w;
-      m = dadd(m, w);
-      cx = dadd(cx, dmul((double)a.x, w));
-      cy = dadd(cy, dmul((double)a.y, w));
-      cz = dadd(cz, dmul((double)a.z, w));
-      const int nk = c.nd[k].m.y;
-      k = nk > k ? nk : end;  // skip pointers always move forward
+    if (c.cdepth[e] < sg.levels) {
+      const int4 s0 = __ldcg(reinterpret_cast<const int4 *>(c.cslot + 8 * e));
+      const int4 s1 = __ldcg(reinterpret_cast<const int4 *>(c.cslot + 8 * e) + 1);
+      const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+#pragma unroll
+      for (int j = 0; j < 8; j++)
+        if (sl[j] > idx && sl[j] < end) add_child(c, sl[j], m, cx, cy, cz);
+    } else {
+      for (int k = idx + 1; k < end;) {
+        add_child(c, k, m, cx, cy, cz);
+        const int nk = c.nd[k].m.y;
+        k = nk > k ? nk : end;  // skip pointers always move forward
+      }
     }
     const float4 r = make_float4(__double2float_rn(ddiv(cx, m)), __double2float_rn(ddiv(cy, m)),
                                  __double2float_rn(ddiv(cz, m)), __double2float_rn(m));
@@ -352,6 +474,79 @@ __global__ void __launch_bounds__(kTB) k_moments(Ctx c, int ntotal)
     if (atomicSub(&c.pending[p], 1) != 1) break;
     __threadfence();
     e = p;
+  }
+}
+
+// Large trees: the same moments one octal depth at a time, deepest first,
+// over a dense list of the cells of each depth, so a warp's 32 lanes work on
+// 32 cells (double arithmetic issues per warp instruction whatever the number
+// of active lanes, and runs at 1/64 of the FP32 rate on this GPU).
+constexpr int kDepthBins = 32;  // octal depths 0 .. kMaxLevels
+
+__global__ void __launch_bounds__(kTB) k_depth_count(Ctx c, int ntotal)
+{
+  __shared__ int h[kDepthBins];
+  if (threadIdx.x < kDepthBins) h[threadIdx.x] = 0;
+  __syncthreads();
+  const int e = blockIdx.x * kTB + threadIdx.x;
+  if (e < ntotal && c.cdepth[e] >= 0) atomicAdd(&h[c.cdepth[e]], 1);
+  __syncthreads();
+  if (threadIdx.x < kDepthBins && h[threadIdx.x]) atomicAdd(&c.lvl[threadIdx.x], h[threadIdx.x]);
+}
+
+// lvl[0..31] counts per depth, lvl[32..63] list start per depth, lvl[64..95] cursors
+__global__ void __launch_bounds__(kTB) k_depth_fill(Ctx c, int ntotal)
+{
+  __shared__ int h[kDepthBins], start[kDepthBins];
+  if (threadIdx.x < kDepthBins) h[threadIdx.x] = 0;
+  __syncthreads();
+  const int e = blockIdx.x * kTB + threadIdx.x;
+  const int d = e < ntotal ? c.cdepth[e] : -1;
+  int rank = 0;
+  if (d >= 0) rank = atomicAdd(&h[d], 1);
+  __syncthreads();
+  if (threadIdx.x < kDepthBins) {
+    int off = 0;
+    for (int k = 0; k < (int)threadIdx.x; k++) off += c.lvl[k];
+    if (blockIdx.x == 0) c.lvl[kDepthBins + threadIdx.x] = off;
+    start[threadIdx.x] = h[threadIdx.x] ? off + atomicAdd(&c.lvl[2 * kDepthBins + threadIdx.x],
+                                                          h[threadIdx.x])
+                                        : 0;
+  }
+  __syncthreads();
+  if (d >= 0) c.cell_list[start[d] + rank] = e;
+}
+
+__global__ void __launch_bounds__(kTB) k_moments_level(Ctx c, int depth)
+{
+  const int count = c.lvl[depth], first = c.lvl[kDepthBins + depth];
+  for (int i = blockIdx.x * kTB + threadIdx.x; i < count; i += gridDim.x * kTB) {
+    const int e = c.cell_list[first + i];
+    const int s = c.sb.hi_a[e];
+    const SegState &sg = c.seg[s];
+    const int idx = c.cidx[e], end = c.cskip[e];
+    if (c.pending[e] == 0) c.nd[idx].m.x |= (int)0x80000000;
+    double m = 0., cx = 0., cy = 0., cz = 0.;
+    if (depth < sg.levels) {
+      const int4 s0 = reinterpret_cast<const int4 *>(c.cslot + 8 * e)[0];
+      const int4 s1 = reinterpret_cast<const int4 *>(c.cslot + 8 * e)[1];
+      const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+#pragma unroll
+      for (int j = 0; j < 8; j++)
+        if (sl[j] > idx && sl[j] < end) add_child(c, sl[j], m, cx, cy, cz);
+    } else {
+      for (int k = idx + 1; k < end;) {
+        add_child(c, k, m, cx, cy, cz);
+        const int nk = c.nd[k].m.y;
+        k = nk > k ? nk : end;  // skip pointers always move forward
+      }
+    }
+    const float4 r = make_float4(__double2float_rn(ddiv(cx, m)), __double2float_rn(ddiv(cy, m)),
+                                 __double2float_rn(ddiv(cz, m)), __double2float_rn(m));
+    c.nd_abs[idx] = r;
+    float4 rel = make_rel(r, sg.fc, c.P);
+    rel.w = -rel.w;  // the sign bit marks a cell for the walks
+    c.nd[idx].p = rel;
   }
 }
 
@@ -390,6 +585,7 @@ void launch_tree_build(Ctx &c, const PassPlan &pl)
   radix_sort(c.sb, n, words, shifts, np, c.st);
   HBTU_CUDA(cudaMemsetAsync(c.mask, 0, sizeof(unsigned long long) * (size_t)n, c.st));
   HBTU_CUDA(cudaMemsetAsync(c.pending, 0, sizeof(int) * (size_t)n, c.st));
+  HBTU_CUDA(cudaMemsetAsync(c.cslot, 0xff, sizeof(int) * 8 * (size_t)n, c.st));
   k_karras<<<nblk(n), kTB, 0, c.st>>>(c, n);
   HBTU_LAUNCHED();
   k_cells<<<nblk(n), kTB, 0, c.st>>>(c, n);
@@ -401,10 +597,22 @@ void launch_tree_build(Ctx &c, const PassPlan &pl)
   HBTU_LAUNCHED();
   k_cellnodes<<<nblk(n), kTB, 0, c.st>>>(c, n);
   HBTU_LAUNCHED();
-  HBTU_CUDA(cudaMemcpyAsync(c.pending0, c.pending, sizeof(int) * (size_t)n,
-                            cudaMemcpyDeviceToDevice, c.st));
-  k_moments<<<nblk(n), kTB, 0, c.st>>>(c, n);
-  HBTU_LAUNCHED();
+  if (n < kLevelSyncMin) {  // small trees: one launch, climbing by atomic countdown
+    HBTU_CUDA(cudaMemcpyAsync(c.pending0, c.pending, sizeof(int) * (size_t)n,
+                              cudaMemcpyDeviceToDevice, c.st));
+    k_moments<<<nblk(n), kTB, 0, c.st>>>(c, n);
+    HBTU_LAUNCHED();
+  } else {  // large trees: dense per-depth cell lists, one launch per depth
+    HBTU_CUDA(cudaMemsetAsync(c.lvl, 0, sizeof(int) * 3 * kDepthBins, c.st));
+    k_depth_count<<<nblk(n), kTB, 0, c.st>>>(c, n);
+    HBTU_LAUNCHED();
+    k_depth_fill<<<nblk(n), kTB, 0, c.st>>>(c, n);
+    HBTU_LAUNCHED();
+    for (int d = pl.max_levels; d >= 0; d--) {
+      k_moments_level<<<152 * 2, kTB, 0, c.st>>>(c, d);
+      HBTU_LAUNCHED();
+    }
+  }
 }
 
 }  // namespace hbtu
