@@ -520,7 +520,7 @@ hbtu_status hbtu_set_option(hbtu_handle *h, const char *name, int64_t value)
     return HBTU_OK;
   }
   if (n == "walk_schedule") {
-    if (value < 0 || value > 4) return fail(h, HBTU_ERR_INVALID_ARGUMENT, "walk_schedule: 0 to 4");
+    if (value != 0 && value != 1) return fail(h, HBTU_ERR_INVALID_ARGUMENT, "walk_schedule: 0 or 1");
     h->opt_schedule = value;
     return HBTU_OK;
   }

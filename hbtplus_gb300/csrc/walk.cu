@@ -346,67 +346,6 @@ __global__ void __launch_bounds__(kB) k_walk_fp32_lean(Ctx c, int total)
   count_interactions(c, t.s, iters - opens);
 }
 
-// FP32 walk, group schedule: the lanes of a warp form groups of G
-// neighbouring targets, and each group visits the union of its targets' walks
-// in increasing index order, so its lanes read one node record together (a
-// broadcast).  The next node needs no reduction: every target of the group
-// not at the current node waits at or beyond its skip pointer (a preorder
-// walk enters a subtree only through its root), so the smallest waiting
-// index is cur + 1 if a target opens cur, else the skip pointer -- unless
-// that leaves the tree (stored as kDone), where the group takes its minimum.
-template <int kB, int G>
-__global__ void __launch_bounds__(kB) k_walk_fp32_group(Ctx c, int total)
-{
-  const DevParams &P = c.P;
-  Target t;
-  load_target<true>(c, blockIdx.x * kB + threadIdx.x, total, t);
-  const float hf = (float)P.h, hinvf = (float)P.h_inv, h2f = hf * hf;
-  const double th2d = (double)P.theta2;
-  const int lim = 2 * c.N + 1;  // node slots
-  const unsigned lane = threadIdx.x & 31u;
-  const unsigned gmask = G == 32 ? 0xffffffffu : ((1u << G) - 1u) << (lane & ~(unsigned)(G - 1));
-  float hi = 0.f, comp = 0.f;  // Kahan sum
-  int ninter = 0;
-  int nxt = t.nxt;
-  int cur = __reduce_min_sync(gmask, nxt);
-  while (cur != kDone) {
-    float4 na;
-    int4 nm;
-    load_node(c.nd, cur, na, nm);
-    const bool act = nxt == cur;
-    const float r2 = dist2(na, t.q);
-    const float lo = __int_as_float(nm.z), up = __int_as_float(nm.w);
-    bool open = r2 < lo;
-    if (act && r2 >= lo && r2 <= up)
-      open = exact_open(na, t.q, __int_as_float(nm.x & 0x7fffffff), th2d);
-    open = open && act;
-    const bool take = act && !open;
-    const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
-    const float mass = fabsf(na.w);
-    float contrib = -mass * rinv;
-    if (take && r2 < h2f) contrib = softened_fp32(mass, r2, rinv, hf, hinvf);
-    contrib = take ? contrib : 0.f;
-    const float y = __fsub_rn(contrib, comp);
-    const float sum = __fadd_rn(hi, y);
-    comp = __fsub_rn(__fsub_rn(sum, hi), y);
-    hi = sum;
-    ninter += take ? 1 : 0;
-    const int sk = nm.y;
-    if (act)
-      nxt = open ? (cur + 1 < t.end ? cur + 1 : kDone)
-                 : ((unsigned)(sk - cur - 1) < (unsigned)(t.end - cur - 1) ? sk : kDone);
-    // selects, not branches: the groups of a warp stay converged
-    const bool anyopen = __any_sync(gmask, open);
-    const bool sk_ok = (unsigned)(sk - cur - 1) < (unsigned)(lim - cur - 1);
-    const int least = max(__reduce_min_sync(gmask, nxt), cur + 1);
-    cur = anyopen ? cur + 1 : (sk_ok ? sk : least);
-    if (cur >= lim) break;
-  }
-  const double base = (double)__fdiv_rn(t.mself, P.eps);  // cancels the self term
-  finish_target(c, t, dadd(dadd(base, (double)hi), -(double)comp));
-  count_interactions(c, t.s, ninter);
-}
-
 // FP64: the reference's arithmetic, operation by operation.
 __global__ void __launch_bounds__(kWB) k_walk_fp64(Ctx c, int total)
 {
@@ -572,20 +511,6 @@ void launch_walk(Ctx &c, const PassPlan &pl)
     k_walk_fp32<true><<<blocks, kWB, 0, c.st>>>(c, n);
   else if (c.opt_schedule == 1)
     k_walk_fp32<false><<<blocks, kWB, 0, c.st>>>(c, n);
-  else if (c.opt_schedule >= 2) {
-    const int G = c.opt_schedule == 2 ? 2 : c.opt_schedule == 3 ? 4 : 8;
-    const int B = n >= 152 * 4 * 512 ? 512 : n >= 152 * 4 * 256 ? 256 : 128;
-    const unsigned bl = (n + B - 1) / B;
-#define HBTU_GROUP_LAUNCH(BB, GG) k_walk_fp32_group<BB, GG><<<bl, BB, 0, c.st>>>(c, n)
-    if (B == 512) {
-      if (G == 2) HBTU_GROUP_LAUNCH(512, 2); else if (G == 4) HBTU_GROUP_LAUNCH(512, 4); else HBTU_GROUP_LAUNCH(512, 8);
-    } else if (B == 256) {
-      if (G == 2) HBTU_GROUP_LAUNCH(256, 2); else if (G == 4) HBTU_GROUP_LAUNCH(256, 4); else HBTU_GROUP_LAUNCH(256, 8);
-    } else {
-      if (G == 2) HBTU_GROUP_LAUNCH(128, 2); else if (G == 4) HBTU_GROUP_LAUNCH(128, 4); else HBTU_GROUP_LAUNCH(128, 8);
-    }
-#undef HBTU_GROUP_LAUNCH
-  }
   else if (n >= 152 * 4 * 512)  // blocks of neighbouring targets share an SM's L1
     k_walk_fp32_lean<512><<<(n + 511) / 512, 512, 0, c.st>>>(c, n);
   else if (n >= 152 * 4 * 256)
