@@ -45,6 +45,36 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
 
+// Exact float -> double and round-to-nearest-even double -> float, built
+// from the IEEE-754 fields with integer operations: the conversion
+// instructions run on the FP64 unit, at 1/64 of the FP32 rate on this GPU.
+// Zero, subnormal, infinite and NaN inputs (and results outside the normal
+// float range) take the conversion instruction.
+__device__ __forceinline__ double f2d(float x)
+{
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long s = (unsigned long long)(u >> 31) << 63;
+  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)s);
+  if (e == 0u || e == 0xffu) return (double)x;
+  return __longlong_as_double((long long)(s | ((unsigned long long)(e + (1023 - 127)) << 52) |
+                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+__device__ __forceinline__ float d2f(double x)
+{
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ffull) - 1023 + 127;
+  if (e <= 0 || e >= 255) return __double2float_rn(x);
+  const unsigned long long mant = b & 0xfffffffffffffull;
+  unsigned long long r = mant >> 29;
+  const unsigned long long rem = mant & 0x1fffffffull, half = 1ull << 28;
+  if (rem > half || (rem == half && (r & 1ull))) r++;
+  const unsigned bits = (unsigned)(((unsigned long long)e << 23) + r);  // a carry bumps the exponent
+  if (((bits >> 23) & 0xffu) == 0xffu) return __double2float_rn(x);
+  return __uint_as_float(bits | ((unsigned)(b >> 63) << 31));
+}
+
 // NEAREST (src/config_parser.h:142) on a double / a float operand.
 __device__ __forceinline__ double nearest_d(double x, const DevParams &P)
 {
@@ -79,9 +109,9 @@ __device__ __forceinline__ float vdot(const float a[3], const float b[3])
 // double, then rounded to float.
 __device__ __forceinline__ float rel_coord(float x, float c, const DevParams &P)
 {
-  double d = dsub((double)x, (double)c);
+  double d = dsub(f2d(x), f2d(c));
   if (P.periodic) d = nearest_d(d, P);
-  return __double2float_rn(d);
+  return d2f(d);
 }
 
 // Order-preserving 32-bit key of a float (ascending); -0 sorts as +0.

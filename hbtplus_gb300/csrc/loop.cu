@@ -376,25 +376,26 @@ __global__ void __launch_bounds__(kLB) k_avg_chunks(Ctx c)
   const int ci = b - c.bchunk_base[s];
   const int lo = ci * kChunk, hi = min(lo + kChunk, nb);
   const float4 o = c.pm[c.epid[sg.off]];
-  const double ox = o.x, oy = o.y, oz = o.z;
+  const double ox = f2d(o.x), oy = f2d(o.y), oz = f2d(o.z);
   double v[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int p = lo + threadIdx.x; p < hi; p += kLB) {
     const int pid = c.epid[sg.off + p];
     const float4 a = c.pm[pid];
     const float4 u = c.vel[pid];
     const float m = a.w;
-    v[0] += (double)m;
-    v[1] += (double)fmul(u.x, m);
-    v[2] += (double)fmul(u.y, m);
-    v[3] += (double)fmul(u.z, m);
+    const double md = f2d(m);
+    v[0] += md;
+    v[1] += f2d(fmul(u.x, m));
+    v[2] += f2d(fmul(u.y, m));
+    v[3] += f2d(fmul(u.z, m));
     if (c.P.periodic) {
-      v[4] += dmul(nearest_d(dsub((double)a.x, ox), c.P), (double)m);
-      v[5] += dmul(nearest_d(dsub((double)a.y, oy), c.P), (double)m);
-      v[6] += dmul(nearest_d(dsub((double)a.z, oz), c.P), (double)m);
+      v[4] += dmul(nearest_d(dsub(f2d(a.x), ox), c.P), md);
+      v[5] += dmul(nearest_d(dsub(f2d(a.y), oy), c.P), md);
+      v[6] += dmul(nearest_d(dsub(f2d(a.z), oz), c.P), md);
     } else {
-      v[4] += (double)fmul(a.x, m);
-      v[5] += (double)fmul(a.y, m);
-      v[6] += (double)fmul(a.z, m);
+      v[4] += f2d(fmul(a.x, m));
+      v[5] += f2d(fmul(a.y, m));
+      v[6] += f2d(fmul(a.z, m));
     }
   }
   block_sum<7>(v, c.chunk_sums + (size_t)b * kSums);
@@ -611,31 +612,33 @@ __global__ void __launch_bounds__(kLB) k_kin_chunks(Ctx c)
   const int lo = ci * kChunk, hi = min(lo + kChunk, nb);
   double v[18];
   for (int k = 0; k < 18; k++) v[k] = 0.;
+  const double Pa = (double)P.a, PHz = (double)P.Hz;
   for (int p = lo + threadIdx.x; p < hi; p += kLB) {
     const int pid = c.epid[sg.off + p];
     const float4 a = c.pm[pid], u = c.vel[pid];
     const float m = a.w;
     const float x[3] = {a.x, a.y, a.z}, w[3] = {u.x, u.y, u.z};
-    v[0] += (double)fmul(c.eE[sg.off + p], m);
+    const double md = f2d(m);
+    v[0] += f2d(fmul(c.eE[sg.off + p], m));
     double dx[3], dv[3];
     for (int j = 0; j < 3; j++) {
-      dx[j] = (double)fsub(x[j], sg.ref_pos[j]);
+      dx[j] = f2d(fsub(x[j], sg.ref_pos[j]));
       if (P.periodic) dx[j] = nearest_d(dx[j], P);
-      dx[j] = dmul(dx[j], (double)P.a);
-      dv[j] = dadd((double)fsub(w[j], sg.ref_vel[j]), dmul((double)P.Hz, dx[j]));
-      v[1] += dmul(dmul(dv[j], dv[j]), (double)m);
+      dx[j] = dmul(dx[j], Pa);
+      dv[j] = dadd(f2d(fsub(w[j], sg.ref_vel[j])), dmul(PHz, dx[j]));
+      v[1] += dmul(dmul(dv[j], dv[j]), md);
     }
-    v[2] += dmul(dsub(dmul(dx[1], dv[2]), dmul(dx[2], dv[1])), (double)m);
-    v[3] += dmul(dsub(dmul(dx[2], dv[0]), dmul(dx[0], dv[2])), (double)m);
-    v[4] += dmul(dsub(dmul(dx[0], dv[1]), dmul(dx[1], dv[0])), (double)m);
-    v[5] += (double)m;
+    v[2] += dmul(dsub(dmul(dx[1], dv[2]), dmul(dx[2], dv[1])), md);
+    v[3] += dmul(dsub(dmul(dx[2], dv[0]), dmul(dx[0], dv[2])), md);
+    v[4] += dmul(dsub(dmul(dx[0], dv[1]), dmul(dx[1], dv[0])), md);
+    v[5] += md;
     const int t = c.type ? c.type[pid] : 1;
     const bool skip = (nb <= 100 && c.id[pid] == -1) || t < 0 || t > 5;
 #pragma unroll
     for (int q = 0; q < 6; q++)
       if (!skip && q == t) {
         v[6 + q] += 1.0;
-        v[12 + q] += (double)m;
+        v[12 + q] += md;
       }
   }
   block_sum<18>(v, c.chunk_sums + (size_t)b * kSums);

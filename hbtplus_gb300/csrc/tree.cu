@@ -430,12 +430,14 @@ __global__ void __launch_bounds__(kTB) k_cellnodes(Ctx c, int ntotal)
 __device__ __forceinline__ void add_child(const Ctx &c, int k, double &m, double &cx, double &cy,
                                           double &cz)
 {
+  // a product of two floats is exact in double, so one fused multiply-add
+  // rounds exactly as the reference's multiply-then-add
   const float4 a = __ldcg(&c.nd_abs[k]);
-  const double w = (double)a.w;
+  const double w = f2d(a.w);
   m = dadd(m, w);
-  cx = dadd(cx, dmul((double)a.x, w));
-  cy = dadd(cy, dmul((double)a.y, w));
-  cz = dadd(cz, dmul((double)a.z, w));
+  cx = __fma_rn(f2d(a.x), w, cx);
+  cy = __fma_rn(f2d(a.y), w, cy);
+  cz = __fma_rn(f2d(a.z), w, cz);
 }
 
 __global__ void __launch_bounds__(kTB) k_moments(Ctx c, int ntotal)
@@ -462,8 +464,7 @@ __global__ void __launch_bounds__(kTB) k_moments(Ctx c, int ntotal)
         k = nk > k ? nk : end;  // skip pointers always move forward
       }
     }
-    const float4 r = make_float4(__double2float_rn(ddiv(cx, m)), __double2float_rn(ddiv(cy, m)),
-                                 __double2float_rn(ddiv(cz, m)), __double2float_rn(m));
+    const float4 r = make_float4(d2f(ddiv(cx, m)), d2f(ddiv(cy, m)), d2f(ddiv(cz, m)), d2f(m));
     __stcg(&c.nd_abs[idx], r);
     float4 rel = make_rel(r, sg.fc, c.P);
     rel.w = -rel.w;  // the sign bit marks a cell for the walks
@@ -541,8 +542,7 @@ __global__ void __launch_bounds__(kTB) k_moments_level(Ctx c, int depth)
         k = nk > k ? nk : end;  // skip pointers always move forward
       }
     }
-    const float4 r = make_float4(__double2float_rn(ddiv(cx, m)), __double2float_rn(ddiv(cy, m)),
-                                 __double2float_rn(ddiv(cz, m)), __double2float_rn(m));
+    const float4 r = make_float4(d2f(ddiv(cx, m)), d2f(ddiv(cy, m)), d2f(ddiv(cz, m)), d2f(m));
     c.nd_abs[idx] = r;
     float4 rel = make_rel(r, sg.fc, c.P);
     rel.w = -rel.w;  // the sign bit marks a cell for the walks
