@@ -107,6 +107,12 @@ SIGNATURES = {
     "hbtu_unbind_noalloc": (C.c_int, [C.POINTER(hbtu_params), C.POINTER(hbtu_particles), C.c_int64,
                                       C.POINTER(hbtu_state), C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p]),
+    "hbtu_index_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "hbtu_index_destroy": (C.c_int, [C.c_void_p]),
+    "hbtu_index_fill": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
+                                  C.c_int32]),
+    "hbtu_index_lookup": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]),
+    "hbtu_index_key_range": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
 }
 
 _LIB = None

@@ -17,24 +17,8 @@
 #include <vector>
 
 #include "driver.h"
+#include "handle.h"
 
-struct hbtu_handle {
-  hbtu_params params;
-  hbtu::DevParams dp;
-  int device = 0;
-  cudaStream_t own_stream = nullptr, stream = nullptr;
-  std::string err;
-  char *ws = nullptr;
-  size_t ws_bytes = 0;
-  hbtu::PassPlan *plan_host = nullptr;
-  // tracing
-  hbtu_stats stats{};
-  bool timing = false;
-  // tuning options (hbtu_set_option)
-  int64_t opt_leaf_runs = 1;
-  int64_t opt_schedule = 0;
-  std::vector<cudaEvent_t> events;  // pool: 4 per pass when timing, 2 per call
-};
 
 namespace hbtu {
 
@@ -566,7 +550,7 @@ hbtu_status hbtu_reset_stats(hbtu_handle *h)
 hbtu_status hbtu_set_stream(hbtu_handle *h, void *cuda_stream)
 {
   if (!h) return HBTU_ERR_INVALID_ARGUMENT;
-  h->stream = cuda_stream ? (cudaStream_t)cuda_stream : h->own_stream;
+  h->stream = (cudaStream_t)cuda_stream;  // NULL: the legacy default stream
   return HBTU_OK;
 }
 

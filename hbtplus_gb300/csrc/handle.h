@@ -1,0 +1,26 @@
+// handle.h -- the state behind an hbtu_handle (include/hbtu.h).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "hbtu_internal.h"
+
+struct hbtu_handle {
+  hbtu_params params;
+  hbtu::DevParams dp;
+  int device = 0;
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  std::string err;
+  char *ws = nullptr;
+  size_t ws_bytes = 0;
+  hbtu::PassPlan *plan_host = nullptr;
+  // tracing
+  hbtu_stats stats{};
+  bool timing = false;
+  // tuning options (hbtu_set_option)
+  int64_t opt_leaf_runs = 1;
+  int64_t opt_schedule = 0;
+  std::vector<cudaEvent_t> events;  // pool: 4 per pass when timing, 2 per call
+};

@@ -114,8 +114,10 @@ typedef struct hbtu_handle hbtu_handle;
 hbtu_status hbtu_create(const hbtu_params *params, hbtu_handle **out);
 hbtu_status hbtu_destroy(hbtu_handle *h);
 
-/* Replace the handle's stream by a caller-owned cudaStream_t (NULL: the
- * handle's own stream). */
+/* Enqueue the handle's work on a caller-owned cudaStream_t from now on.
+ * NULL is CUDA's legacy default stream (what a framework's "current stream"
+ * is by default), so work there is ordered with the caller's.  A new handle
+ * uses a stream of its own. */
 hbtu_status hbtu_set_stream(hbtu_handle *h, void *cuda_stream);
 
 /* Unbind one subhalo: Subhalo_t::Unbind (src/subhalo_unbind.cpp:263-431).
@@ -232,6 +234,33 @@ hbtu_status hbtu_energy_gradient(hbtu_handle *h, const hbtu_particles *p, int64_
  * host memory; p follows p->location. */
 hbtu_status hbtu_direct_potential(hbtu_handle *h, const hbtu_particles *p, int64_t n,
                                   const int64_t *targets, int64_t ntarget, double *potential_out);
+
+/* Particle-ID -> index tables, the ID re-resolve of the unbinding step's
+ * callers (IndexTable_t, src/hash.h:47-112; filled from a snapshot's IDs by
+ * ParticleSnapshot_t, src/snapshot.h:191-224, and queried by GetIndex /
+ * GetIndices, src/hash.tpp:47-55 / src/hash_remote.tpp:5-99).  A table lives
+ * on the handle's device and uses its stream.
+ *   flat = 0: MappedIndexTable_t -- pairs sorted by key, binary search per
+ *             query; a negative key is absent;
+ *   flat = 1: FlatIndexTable_t -- a dense array over [KeyMin, KeyMax] (key
+ *             spans above 2^32 are refused: HBTU_ERR_TOO_LARGE).
+ * Duplicate keys (undefined in the reference): the first pair in input order
+ * wins in a mapped table, the last in a flat table. */
+typedef struct hbtu_index_table hbtu_index_table;
+hbtu_status hbtu_index_create(hbtu_handle *h, int32_t flat, hbtu_index_table **out);
+hbtu_status hbtu_index_destroy(hbtu_index_table *t);
+/* IndexTable_t::Fill(Keys, null_index) (src/hash.tpp:18-30, :59-95): the
+ * pairs (keys[i], values[i]), i < n (KeyList_t::GetKey / ::GetIndex); both
+ * arrays in host (location HBTU_HOST) or device memory. */
+hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int64_t *values,
+                            int64_t n, int64_t null_index, int32_t location);
+/* GetIndex for every query: out[j] = the value paired with keys[j], or the
+ * null index (GetIndices, any query order); keys and out in host or device
+ * memory as location says. */
+hbtu_status hbtu_index_lookup(hbtu_index_table *t, const int64_t *keys, int64_t m, int64_t *out,
+                              int32_t location);
+/* GetKeyMinMax (src/hash.h:88-93, :102-107); max < min for an empty table. */
+hbtu_status hbtu_index_key_range(const hbtu_index_table *t, int64_t *key_min, int64_t *key_max);
 
 /* Message of the last failed call on this handle (or of the last failed
  * hbtu_create when h is NULL). */

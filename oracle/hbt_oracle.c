@@ -844,3 +844,81 @@ int hbto_binding_energies(const hbto_params *par, int64_t n, const float *pos, c
 }
 
 void hbto_srand48(long seed) { srand48(seed); }
+
+/* ------------------------------------------------------------------ ID tables */
+
+typedef struct {
+  int64_t key, pos;
+} keypos;
+
+static int cmp_keypos(const void *a, const void *b)
+{
+  const keypos *x = (const keypos *)a, *y = (const keypos *)b;
+  if (x->key != y->key) return x->key < y->key ? -1 : 1;
+  return x->pos < y->pos ? -1 : (x->pos > y->pos); /* first in input order first */
+}
+
+/* MappedIndexTable_t::Fill (hash.tpp:18-30): the (key, index) pairs sorted by
+ * key; GetIndex (hash.tpp:47-55): a negative key is absent, else binary search. */
+static void mapped_lookup(const int64_t *keys, const int64_t *values, int64_t n, int64_t null_index,
+                          const int64_t *queries, int64_t m, int64_t *out)
+{
+  keypos *map = malloc((n > 0 ? n : 1) * sizeof(keypos));
+  for (int64_t i = 0; i < n; i++) {
+    map[i].key = keys[i];
+    map[i].pos = i;
+  }
+  qsort(map, (size_t)n, sizeof(keypos), cmp_keypos);
+  for (int64_t j = 0; j < m; j++) {
+    const int64_t q = queries[j];
+    out[j] = null_index;
+    if (q < 0) continue;
+    int64_t lo = 0, hi = n; /* lower_bound */
+    while (lo < hi) {
+      const int64_t mid = lo + (hi - lo) / 2;
+      if (map[mid].key < q)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    if (lo < n && map[lo].key == q) out[j] = values[map[lo].pos];
+  }
+  free(map);
+}
+
+/* FlatIndexTable_t::Fill (hash.tpp:59-95): a dense array over [KeyMin, KeyMax]
+ * set to null, then Index[key] = index for every pair; GetIndex
+ * (hash.tpp:104-109): null outside [KeyMin, KeyMax]. */
+static void flat_lookup(const int64_t *keys, const int64_t *values, int64_t n, int64_t null_index,
+                        const int64_t *queries, int64_t m, int64_t *out)
+{
+  if (n == 0) {
+    for (int64_t j = 0; j < m; j++) out[j] = null_index;
+    return;
+  }
+  int64_t kmin = keys[0], kmax = keys[0];
+  for (int64_t i = 1; i < n; i++) {
+    if (keys[i] > kmax) kmax = keys[i];
+    if (keys[i] < kmin) kmin = keys[i];
+  }
+  const int64_t span = kmax - kmin + 1;
+  int64_t *index = malloc((size_t)span * sizeof(int64_t));
+  for (int64_t k = 0; k < span; k++) index[k] = null_index;
+  for (int64_t i = 0; i < n; i++) index[keys[i] - kmin] = values[i];
+  for (int64_t j = 0; j < m; j++) {
+    const int64_t q = queries[j];
+    out[j] = (q < kmin || q > kmax) ? null_index : index[q - kmin];
+  }
+  free(index);
+}
+
+int hbto_index_lookup(int flat, const int64_t *keys, const int64_t *values, int64_t n,
+                      int64_t null_index, const int64_t *queries, int64_t m, int64_t *out)
+{
+  if (n < 0 || m < 0) return -1;
+  if (flat)
+    flat_lookup(keys, values, n, null_index, queries, m, out);
+  else
+    mapped_lookup(keys, values, n, null_index, queries, m, out);
+  return 0;
+}

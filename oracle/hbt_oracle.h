@@ -118,6 +118,20 @@ void hbto_srand48(long seed);
  * (src/subhalo_unbind.cpp:302): perm[i] = original index now at i. */
 void hbto_reference_shuffle(int64_t n, unsigned seed, int64_t *perm);
 
+/* Particle-ID -> index tables (src/hash.h:47-112, src/hash.tpp, src/hash_remote.tpp).
+ * Fill a table with the pairs (keys[i], values[i]), i < n (KeyList_t::GetKey and
+ * ::GetIndex), then look up every query: out[j] = GetIndex(queries[j]), or
+ * null_index when the key is absent.
+ *   flat = 0: MappedIndexTable_t -- pairs sorted by key, binary search; a
+ *             negative key is absent (hash.tpp:18-55);
+ *   flat = 1: FlatIndexTable_t -- a dense array over [KeyMin, KeyMax]
+ *             (hash.tpp:59-109).
+ * Duplicate keys are not defined by the reference (std::sort is not stable,
+ * and the flat fill writes in parallel); here the first pair in input order
+ * wins for the mapped table and the last for the flat one. */
+int hbto_index_lookup(int flat, const int64_t *keys, const int64_t *values, int64_t n,
+                      int64_t null_index, const int64_t *queries, int64_t m, int64_t *out);
+
 #ifdef __cplusplus
 }
 #endif

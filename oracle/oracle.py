@@ -137,6 +137,29 @@ class Oracle:
         self._shuffle(n, seed, _p(perm, C.c_int64))
         return perm[:n]
 
+    def index_lookup(self, keys, values, queries, flat: bool = False, null_index: int = -1,
+                     batch: bool = False) -> np.ndarray:
+        """Fill a particle-ID table with (keys, values) and look up every query
+        (MappedIndexTable_t / FlatIndexTable_t, src/hash.tpp).  batch=True uses
+        the reference's GetIndices (reference build only; the mapped table
+        expects ascending queries)."""
+        k = np.ascontiguousarray(keys, np.int64)
+        v = np.ascontiguousarray(values, np.int64)
+        q = np.ascontiguousarray(queries, np.int64)
+        out = np.empty(max(len(q), 1), np.int64)
+        if batch:
+            if not self.reference:
+                raise ValueError("the batch form exists in the reference build only")
+            fn = self.lib.ref_index_lookup_batch
+        else:
+            fn = getattr(self.lib, ("ref_" if self.reference else "hbto_") + "index_lookup")
+        fn.restype = C.c_int
+        rc = fn(C.c_int(1 if flat else 0), _p(k, C.c_int64), _p(v, C.c_int64), C.c_int64(len(k)),
+                C.c_int64(null_index), _p(q, C.c_int64), C.c_int64(len(q)), _p(out, C.c_int64))
+        if rc != 0:
+            raise RuntimeError(f"index lookup failed ({rc})")
+        return out[:len(q)]
+
     def partition(self, E: np.ndarray):
         E = np.ascontiguousarray(E, np.float32).copy()
         idx = np.arange(len(E), dtype=np.int64)

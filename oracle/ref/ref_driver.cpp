@@ -27,6 +27,8 @@
 #include "gravity_tree.h"
 #include "snapshot.h"
 #include "subhalo.h"
+#include "hash.h"
+#include "hash_remote.tpp"
 
 #include "../hbt_oracle.h"
 
@@ -164,9 +166,65 @@ void sorted_ids(int64_t n, const int64_t *id, std::vector<int64_t> &ids, std::ve
   }
 }
 
+/* The (key, index) pairs handed to IndexTable_t::Fill (src/hash.h:10-17). */
+class ArrayKeyList_t : public KeyList_t<HBTInt, HBTInt>
+{
+  const int64_t *keys_, *values_;
+  HBTInt n_;
+
+public:
+  ArrayKeyList_t(const int64_t *k, const int64_t *v, int64_t n) : keys_(k), values_(v), n_(n) {}
+  HBTInt GetKey(const HBTInt i) const { return keys_[i]; }
+  HBTInt GetIndex(const HBTInt i) const { return values_[i]; }
+  HBTInt size() const { return n_; }
+};
+
+/* A list of particles as GetIndices takes it: elements with an Id field. */
+struct IdOnly_t {
+  HBTInt Id;
+};
+
 }  // namespace
 
 extern "C" {
+
+/* The reference's own tables: Fill, then GetIndex per query (src/hash.tpp). */
+int ref_index_lookup(int flat, const int64_t *keys, const int64_t *values, int64_t n,
+                     int64_t null_index, const int64_t *queries, int64_t m, int64_t *out)
+{
+  ArrayKeyList_t list(keys, values, n);
+  if (flat) {
+    FlatIndexTable_t<HBTInt, HBTInt> table;
+    table.Fill(list, null_index);
+    for (int64_t j = 0; j < m; j++) out[j] = table.GetIndex(queries[j]);
+  } else {
+    MappedIndexTable_t<HBTInt, HBTInt> table;
+    table.Fill(list, null_index);
+    for (int64_t j = 0; j < m; j++) out[j] = table.GetIndex(queries[j]);
+  }
+  return 0;
+}
+
+/* The batch form, GetIndices (src/hash_remote.tpp:5-99); the mapped table's
+ * recursive search expects the queries in ascending order. */
+int ref_index_lookup_batch(int flat, const int64_t *keys, const int64_t *values, int64_t n,
+                           int64_t null_index, const int64_t *queries, int64_t m, int64_t *out)
+{
+  ArrayKeyList_t list(keys, values, n);
+  std::vector<IdOnly_t> parts(m);
+  for (int64_t j = 0; j < m; j++) parts[j].Id = queries[j];
+  if (flat) {
+    FlatIndexTable_t<HBTInt, HBTInt> table;
+    table.Fill(list, null_index);
+    table.GetIndices(parts);
+  } else {
+    MappedIndexTable_t<HBTInt, HBTInt> table;
+    table.Fill(list, null_index);
+    table.GetIndices(parts);
+  }
+  for (int64_t j = 0; j < m; j++) out[j] = parts[j].Id;
+  return 0;
+}
 
 int ref_unbind(const hbto_params *par, int64_t n, const int64_t *id, const float *pos,
                const float *vel, const float *mass, const int32_t *type, const hbto_state *st,

@@ -8,7 +8,9 @@ compressed .npz per case into tests/golden/.  Each file holds the inputs
 (particles in the order Unbind receives them, frame, parameters) and the
 reference's outputs (permuted particle order as input indices, Energies,
 Nbound, Mbound, frames, kinematics, per-type counts); `first_pass_*` cases hold
-the reference tree's BindingEnergy/EvaluatePotential of every particle.
+the reference tree's BindingEnergy/EvaluatePotential of every particle;
+`index_*` cases hold the reference's particle-ID tables and their lookups
+(`python tests/golden/make_golden.py index` writes only those).
 
 For sampled cases the stored particles are the ones AFTER the reference's
 random_shuffle (what the GPU library and the C oracle take), with
@@ -112,5 +114,30 @@ def main():
     print(f"batch_48: n={b['offsets'][-1]}")
 
 
+def index_cases(ref):
+    """Particle-ID tables (src/hash.tpp): the reference's MappedIndexTable_t
+    and FlatIndexTable_t filled with (id, index) pairs, and their answers to
+    queries that hit, miss, fall outside the key range or are negative."""
+    rng = np.random.Generator(np.random.PCG64(115))
+    n = 20000
+    ids = rng.choice(10 * n, n, replace=False).astype(np.int64) + 12345  # sparse ids
+    vals = rng.permutation(n).astype(np.int64)
+    q = np.concatenate([ids[rng.integers(0, n, 5000)], rng.integers(-50, 10 * n + 20000, 5000),
+                        np.array([-1, 0, 12344, 12345, ids.min(), ids.max(), ids.max() + 1])])
+    q = q.astype(np.int64)
+    for flat, name in ((False, "index_mapped"), (True, "index_flat")):
+        out = ref.index_lookup(ids, vals, q, flat=flat, null_index=-1)
+        qs = np.sort(q)
+        outs = ref.index_lookup(ids, vals, qs, flat=flat, null_index=-1, batch=True)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), keys=ids, values=vals,
+                            queries=q, ref_out=out, sorted_queries=qs, ref_out_sorted=outs,
+                            null_index=np.int64(-1))
+        print(f"{name}: {n} keys, {len(q)} queries, {int(np.sum(out != -1))} hits")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["index"]:
+        index_cases(Oracle(reference=True))
+    else:
+        main()
+        index_cases(Oracle(reference=True))
