@@ -58,10 +58,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nsub", type=int, default=2000)
-    ap.add_argument("--workload", default="batch", choices=["batch", "single", "host2e7"],
+    ap.add_argument("--workload", default="batch", choices=["batch", "single", "host2e7", "step"],
                     help="batch: the 2000-subhalo batch (default); single: the isolated "
                          "1e5-particle NFW subhalo (+10%% contaminants); host2e7: the "
-                         "2e7-particle host with 300 clumps (+5%% contaminants)")
+                         "2e7-particle host with 300 clumps (+5%% contaminants); step: a "
+                         "tracking step of 20,000 subhaloes in a 3e7-particle snapshot (ID "
+                         "re-resolve, gather, unbind)")
     ap.add_argument("--open-angle", type=float, default=0.45)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--leaf-runs", type=int, default=-1,
@@ -197,6 +199,11 @@ def measured_peaks():
 def run_reference_arm(args, ws, rank):
     if rank != 0:
         return
+    if args.workload in ("step", "host2e7"):
+        print(json.dumps({"impl": "reference", "unavailable":
+                          f"the {args.workload} workload has no CPU reference run: one pass "
+                          "of the reference over it takes minutes on the host"}), flush=True)
+        return
     batch, params = workload(args.nsub, 0, args.workload, args.open_angle)
     threads = cpu_threads()
     for _ in range(args.warmup):
@@ -242,6 +249,127 @@ def config_of(args, batch):
             "l2": "flushed before each timed step (256 MB write)"}
 
 
+def run_tracking_step(args, ws, rank, local):
+    """The tracking step of 20,000 subhaloes (2000-subhalo law) in a 3e7-particle,
+    200 Mpc/h snapshot: the snapshot's ID table, the re-resolve of every
+    subhalo's particle IDs after a drift and 10% outer stripping, the gather and
+    the batched unbinding, all on the GPU."""
+    import torch
+
+    from hbtplus_gb300 import _lib
+    from hbtplus_gb300 import synthetic as S
+    from hbtplus_gb300.step import TrackingStep
+    from hbtplus_gb300.unbind import Unbinder
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    d = S.tracking_snapshot(seed=20261207 + 1000 * rank)
+    params = S.default_params(box_size=200.0)
+    nsub = len(d["offsets"]) - 1
+    nmem = int(d["offsets"][-1])
+    nsnap = len(d["snap_id"])
+    ub = Unbinder(params, device=local)
+    step = TrackingStep(ub)
+    T = {k: torch.from_numpy(np.ascontiguousarray(d[k])).to(dev)
+         for k in ("snap_id", "snap_pos", "snap_vel", "snap_mass", "snap_type", "member_id")}
+    frames = {k: d[k] for k in ("offsets", "ref_pos", "ref_vel", "mostbound_pos",
+                                "mostbound_vel", "mostbound_id")}
+    states = ub.make_states(frames)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def one():
+        step.load_snapshot(T["snap_id"], T["snap_pos"], T["snap_vel"], T["snap_mass"],
+                           T["snap_type"])
+        return step.run(d["offsets"], T["member_id"], states)
+
+    for _ in range(args.warmup):
+        one()
+    torch.cuda.synchronize()
+    ub.set_timing(True)
+    ub.reset_stats()
+    times, phase = [], []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            e[0].record(stream)
+            step.load_snapshot(T["snap_id"], T["snap_pos"], T["snap_vel"], T["snap_mass"],
+                               T["snap_type"])
+            e[1].record(stream)
+            index = step.resolve(T["member_id"])
+            batch = step.gather(index)
+            e[2].record(stream)
+            out = dict(order=torch.empty(nmem, dtype=torch.int64, device=dev),
+                       energy=torch.empty(nmem, dtype=torch.float32, device=dev),
+                       res=torch.empty(nsub * C.sizeof(_lib.hbtu_result), dtype=torch.uint8,
+                                       device=dev))
+            ub.unbind_batch_device(batch, d["offsets"], states, out)
+            e[3].record(stream)
+            times.append(e)
+        torch.cuda.synchronize()
+    ms = [a[0].elapsed_time(a[3]) for a in times]
+    fill_ms = statistics.mean(a[0].elapsed_time(a[1]) for a in times)
+    rg_ms = statistics.mean(a[1].elapsed_time(a[2]) for a in times)
+    un_ms = statistics.mean(a[2].elapsed_time(a[3]) for a in times)
+    ms_per_step = sum(ms) / args.steps
+    st = ub.stats()
+    clocks = clk.summary()
+    # e2e: snapshot and member IDs from pinned host memory, results back to the host
+    pin = {k: v.cpu().pin_memory() for k, v in T.items()}
+    res_host = torch.empty(nsub * C.sizeof(_lib.hbtu_result), dtype=torch.uint8).pin_memory()
+    order_host = torch.empty(nmem, dtype=torch.int64).pin_memory()
+    e2e_t = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        G = {k: v.to(dev, non_blocking=True) for k, v in pin.items()}
+        step.load_snapshot(G["snap_id"], G["snap_pos"], G["snap_vel"], G["snap_mass"],
+                           G["snap_type"])
+        out, _ = step.run(d["offsets"], G["member_id"], states)
+        order_host.copy_(out["order"], non_blocking=True)
+        res_host.copy_(out["res"], non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_t) / args.steps
+    h2d = sum(int(v.numel() * v.element_size()) for v in pin.values())
+    d2h = nmem * 8 + nsub * C.sizeof(_lib.hbtu_result)
+    # HBM view of the re-resolve + gather phase: per member 8 B id + 8 B index
+    # written and read back + 40 B particle read and written
+    rg_bytes = nmem * (8 + 8 + 8 + 40 + 40)
+    peaks, peak_kind = measured_peaks()
+    line = {
+        "metric": "subhalo unbinds/s in a tracking step (ID re-resolve + gather + unbind)",
+        "value": ws * nsub / (ms_per_step / 1e3), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded: 2000-subhalo law, uniform background, drift, stripping)",
+        "config": {"workload": "tracking step: 20,000 subhaloes, 3e7-particle 200 Mpc/h "
+                               "snapshot, v*dt drift, 10% outer stripping, mapped ID table",
+                   "nsub": nsub, "members": nmem, "snapshot_particles": nsnap,
+                   "l2": "flushed before each timed step (256 MB write)"},
+        "phase_ms_per_step": {"table_fill": fill_ms, "resolve_gather": rg_ms, "unbind": un_ms,
+                              "tree": st["tree_ms"] / args.steps,
+                              "walk": st["walk_ms"] / args.steps},
+        "roofline": {"kernel": "ID re-resolve + gather phase", "bound": "hbm",
+                     "achieved": rg_bytes / (rg_ms / 1e3) / 1e9, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": rg_bytes / (rg_ms / 1e3) / 1e9 / peaks["hbm_gbs"],
+                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": None, "algorithmic_bytes": rg_bytes},
+        "cpu_baseline": None,
+        "cpu_baseline_note": "not measured for this workload (one reference pass over it "
+                             "takes minutes on the host)",
+        "e2e": {"value": ws * nsub / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s},
+        "gpu_launches": int(st["kernel_launches"]) // max(1, args.steps),
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    step.close()
+    ub.close()
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
@@ -250,6 +378,12 @@ def main():
         dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
     if args.impl == "reference":
         run_reference_arm(args, ws, rank)
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    if args.workload == "step":
+        run_tracking_step(args, ws, rank, local)
         if ws > 1:
             import torch.distributed as dist
             dist.destroy_process_group()

@@ -258,3 +258,62 @@ def split(batch: dict, s: int) -> dict:
         sub[k] = batch[k][s]
     sub["mostbound_id"] = int(batch["mostbound_id"][s])
     return sub
+
+
+def tracking_snapshot(nsub: int = 20_000, ntot: int = 30_000_000, box: float = 200.0,
+                      seed: int = 20261207, drift: float = 1e-4, strip: float = 0.1) -> dict:
+    """A tracking step's inputs: the new snapshot and the subhaloes of the last one.
+
+    The subhaloes of the 2000-subhalo law, nsub of them in a `box` Mpc/h box,
+    plus uniform background particles up to `ntot`.  Particle IDs are a sparse
+    random permutation (3 * k + 1), so the ID table is a mapped one.  The new
+    snapshot moves every particle by v * drift (Mpc/h per km/s, periodic) and
+    stores particles in a fresh random order, so the subhaloes' particle IDs
+    must be re-resolved.  Each subhalo keeps the inner (1 - strip) of its
+    particles (by distance to its frame centre; its first particle, the
+    previous most-bound one, stays first).
+
+    Returns dict(snap_id, snap_pos, snap_vel, snap_mass, snap_type: the new
+    snapshot, in its own order; offsets, member_id: each subhalo's particle IDs;
+    ref_pos, ref_vel, mostbound_pos, mostbound_vel, mostbound_id: the frames
+    the unbinding starts from)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    subs = subhalo_batch(nsub=nsub, seed=seed + 1, box=box)
+    nin = int(subs["offsets"][-1])
+    nbg = max(0, ntot - nin)
+    ntot = nin + nbg
+    pos = np.concatenate([subs["pos"], rng.uniform(0.0, box, size=(nbg, 3)).astype(np.float32)])
+    vel = np.concatenate([subs["vel"],
+                          rng.normal(scale=300.0, size=(nbg, 3)).astype(np.float32)])
+    mass = np.concatenate([subs["mass"], np.full(nbg, 1e-4, np.float32)])
+    typ = np.concatenate([subs["type"], np.ones(nbg, np.int32)])
+    ids = rng.permutation(ntot).astype(np.int64) * 3 + 1
+    # the last snapshot's membership, stripped of each subhalo's outer particles
+    off = subs["offsets"]
+    keep_off = [0]
+    members = []
+    for s in range(nsub):
+        o0, o1 = int(off[s]), int(off[s + 1])
+        n = o1 - o0
+        if n == 0:
+            keep_off.append(keep_off[-1])
+            continue
+        d = pos[o0:o1].astype(np.float64) - subs["ref_pos"][s].astype(np.float64)
+        d -= box * np.round(d / box)
+        r2 = np.einsum("ij,ij->i", d, d)
+        nkeep = max(1, int(round((1.0 - strip) * n)))
+        order = np.argsort(r2[1:], kind="stable")[: nkeep - 1] + 1
+        idx = np.concatenate([[0], np.sort(order)]) + o0
+        members.append(ids[idx])
+        keep_off.append(keep_off[-1] + len(idx))
+    # the new snapshot: drifted, in a new order
+    newpos = np.mod(pos + vel * np.float32(drift), np.float32(box)).astype(np.float32)
+    newpos = np.where(newpos >= np.float32(box), np.float32(0.0), newpos)
+    perm = rng.permutation(ntot)
+    return dict(snap_id=ids[perm], snap_pos=newpos[perm], snap_vel=vel[perm],
+                snap_mass=mass[perm], snap_type=typ[perm],
+                offsets=np.array(keep_off, np.int64),
+                member_id=np.concatenate(members) if members else np.zeros(0, np.int64),
+                ref_pos=subs["ref_pos"], ref_vel=subs["ref_vel"],
+                mostbound_pos=subs["mostbound_pos"], mostbound_vel=subs["mostbound_vel"],
+                mostbound_id=ids[off[:-1]].astype(np.int64))
