@@ -160,6 +160,49 @@ class Oracle:
             raise RuntimeError(f"index lookup failed ({rc})")
         return out[:len(q)]
 
+    def recursive_unbind(self, params: dict, forest: dict, relax: float = 3.0):
+        """The reference's RecursiveUnbind over a forest, then TruncateSource
+        (reference build only).  forest: parts (id, pos, vel, mass, type),
+        list_off, nbound_prev, nest_off, nest_idx, roots and the frames.
+        Returns (final list offsets, positions into the input rows, results)."""
+        if not self.reference:
+            raise ValueError("the forest entry exists in the reference build only")
+        lo = np.ascontiguousarray(forest["list_off"], np.int64)
+        nsub = len(lo) - 1
+        ntot = int(lo[-1])
+        ids = np.ascontiguousarray(forest["id"], np.int64)
+        pos = np.ascontiguousarray(forest["pos"], np.float32).reshape(-1)
+        vel = np.ascontiguousarray(forest["vel"], np.float32).reshape(-1)
+        mass = np.ascontiguousarray(forest["mass"], np.float32)
+        typ = np.ascontiguousarray(forest["type"], np.int32)
+        nbp = np.ascontiguousarray(forest["nbound_prev"], np.int64)
+        no = np.ascontiguousarray(forest["nest_off"], np.int64)
+        ni = np.ascontiguousarray(forest["nest_idx"], np.int64)
+        roots = np.ascontiguousarray(forest["roots"], np.int64)
+        sts = (State * max(nsub, 1))()
+        for s in range(nsub):
+            for j in range(3):
+                sts[s].ref_pos[j] = float(forest["ref_pos"][s][j])
+                sts[s].ref_vel[j] = float(forest["ref_vel"][s][j])
+                sts[s].mostbound_pos[j] = float(forest["mostbound_pos"][s][j])
+                sts[s].mostbound_vel[j] = float(forest["mostbound_vel"][s][j])
+            sts[s].mostbound_id = int(forest["mostbound_id"][s])
+        out_off = np.zeros(nsub + 1, np.int64)
+        cap = max(ntot * max(nsub, 1), 1)  # a particle can end in several lists
+        out_pos = np.zeros(cap, np.int64)
+        res = (Result * max(nsub, 1))()
+        par = make_params(params)
+        fn = self.lib.ref_recursive_unbind
+        fn.restype = C.c_int
+        rc = fn(C.byref(par), C.c_double(relax), C.c_int64(nsub), _p(lo, C.c_int64),
+                _p(ids, C.c_int64), _p(pos, C.c_float), _p(vel, C.c_float), _p(mass, C.c_float),
+                _p(typ, C.c_int32), _p(nbp, C.c_int64), sts, _p(no, C.c_int64),
+                _p(ni, C.c_int64), C.c_int64(len(roots)), _p(roots, C.c_int64),
+                _p(out_off, C.c_int64), _p(out_pos, C.c_int64), C.c_int64(cap), res)
+        if rc != 0:
+            raise RuntimeError(f"ref_recursive_unbind failed ({rc})")
+        return out_off, out_pos[:out_off[-1]], [result_dict(res[s]) for s in range(nsub)]
+
     def partition(self, E: np.ndarray):
         E = np.ascontiguousarray(E, np.float32).copy()
         idx = np.arange(len(E), dtype=np.int64)

@@ -188,6 +188,54 @@ struct IdOnly_t {
 
 extern "C" {
 
+/* RecursiveUnbind over a forest of subhaloes, then TruncateSource on all
+ * (src/subhalo_unbind.cpp:432-458, the non-INCLUSIVE_MASS branch of
+ * RefineParticles, :475-515): subhalo s starts with its own particles
+ * own[list_off[s] .. list_off[s+1]), the Nbound of the last snapshot
+ * (nbound_prev[s]; <= 1 makes it an orphan) and its nested subhaloes
+ * nest_idx[nest_off[s] .. nest_off[s+1]); roots[] are unbound in order.
+ * Output: each subhalo's final particle list as positions into the input
+ * arrays (out_off[nsub+1], out_pos[out_capacity]; a tail handed to a host
+ * can stay in the satellite's truncated list too), and its results. */
+int ref_recursive_unbind(const hbto_params *par, double relax_factor, int64_t nsub,
+                         const int64_t *list_off, const int64_t *id, const float *pos,
+                         const float *vel, const float *mass, const int32_t *type,
+                         const int64_t *nbound_prev, const hbto_state *st,
+                         const int64_t *nest_off, const int64_t *nest_idx, int64_t nroot,
+                         const int64_t *roots, int64_t *out_off, int64_t *out_pos,
+                         int64_t out_capacity, hbto_result *res)
+{
+  setup(par);
+  HBTConfig.SourceSubRelaxFactor = relax_factor;
+  omp_set_num_threads(1);
+  omp_set_max_active_levels(1);
+  Epoch_t epoch(par);
+  SubhaloList_t subs(nsub);
+  for (int64_t s = 0; s < nsub; s++) {
+    const int64_t o = list_off[s], n = list_off[s + 1] - o;
+    fill_subhalo(subs[s], n, id + o, pos + 3 * o, vel + 3 * o, mass + o, type ? type + o : nullptr,
+                 st + s);
+    subs[s].Nbound = nbound_prev[s];
+    subs[s].NestedSubhalos.assign(nest_idx + nest_off[s], nest_idx + nest_off[s + 1]);
+  }
+  srand(0);
+  for (int64_t r = 0; r < nroot; r++) subs[roots[r]].RecursiveUnbind(subs, epoch);
+  for (int64_t s = 0; s < nsub; s++) subs[s].TruncateSource();
+  const int64_t ntot = list_off[nsub];
+  std::vector<int64_t> ids, ipos;
+  sorted_ids(ntot, id, ids, ipos);
+  out_off[0] = 0;
+  for (int64_t s = 0; s < nsub; s++) {
+    const int64_t n = subs[s].Particles.size();
+    if (out_off[s] + n > out_capacity) return -1;  // lists may share particles: ask for more
+    std::vector<float> en(n);
+    read_subhalo(subs[s], n, ipos.data(), ids.data(), out_pos + out_off[s], en.data(), res + s,
+                 ntot);
+    out_off[s + 1] = out_off[s] + n;
+  }
+  return 0;
+}
+
 /* The reference's own tables: Fill, then GetIndex per query (src/hash.tpp). */
 int ref_index_lookup(int flat, const int64_t *keys, const int64_t *values, int64_t n,
                      int64_t null_index, const int64_t *queries, int64_t m, int64_t *out)

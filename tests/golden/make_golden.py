@@ -10,7 +10,9 @@ reference's outputs (permuted particle order as input indices, Energies,
 Nbound, Mbound, frames, kinematics, per-type counts); `first_pass_*` cases hold
 the reference tree's BindingEnergy/EvaluatePotential of every particle;
 `index_*` cases hold the reference's particle-ID tables and their lookups
-(`python tests/golden/make_golden.py index` writes only those).
+(`python tests/golden/make_golden.py index` writes only those); `forest_10`
+holds the reference's RecursiveUnbind + TruncateSource over a forest of nested
+subhaloes (`... forest`).
 
 For sampled cases the stored particles are the ones AFTER the reference's
 random_shuffle (what the GPU library and the C oracle take), with
@@ -135,9 +137,79 @@ def index_cases(ref):
         print(f"{name}: {n} keys, {len(q)} queries, {int(np.sum(out != -1))} hits")
 
 
+
+
+
+def forest_case(seed=116, n_scale=1.0):
+    """A forest of nested subhaloes for RecursiveUnbind: two haloes with
+    satellites nested three deep, an orphan with a satellite, a satellite that
+    disrupts, and a field subhalo.  Satellites sit inside their host's volume
+    with their own bulk velocity, so tails do feed the hosts."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    box = 100.0
+    specs = [  # (n, r200, host, offset from host centre, bulk speed, nbound_prev)
+        (4000, 0.25, None, 0.0, 0.0, 4000),     # 0: central of halo A
+        (1500, 0.12, 0, 0.10, 250.0, 1500),     # 1: satellite of 0
+        (600, 0.07, 1, 0.04, 150.0, 600),       # 2: satellite of 1
+        (300, 0.05, 2, 0.02, 120.0, 300),       # 3: satellite of 2 (depth 3)
+        (1, 0.01, 0, 0.15, 0.0, 1),             # 4: orphan in 0
+        (400, 0.06, 4, 0.03, 100.0, 400),       # 5: satellite of the orphan
+        (250, 0.05, 0, 0.12, 300.0, 250),       # 6: a satellite that disrupts (hot)
+        (2500, 0.2, None, 0.0, 0.0, 2500),      # 7: central of halo B
+        (800, 0.09, 7, 0.08, 200.0, 800),       # 8: satellite of 7
+        (700, 0.08, None, 0.0, 0.0, 700),       # 9: field subhalo
+    ]
+    centres, subs = [], []
+    for k, (n, r200, host, off, bulk, _) in enumerate(specs):
+        n = max(1, int(n * n_scale)) if n > 1 else 1
+        if host is None:
+            c = rng.uniform(10.0, 90.0, size=3)
+            v = np.zeros(3)
+        else:
+            u = rng.normal(size=3)
+            c = centres[host][0] + off * u / np.linalg.norm(u)
+            w = rng.normal(size=3)
+            v = centres[host][1] + bulk * w / np.linalg.norm(w)
+        centres.append((c, v))
+        subs.append(S.nfw_subhalo(rng, n, r200, 8.0, contaminant_frac=0.1 if n > 1 else 0.0,
+                                  center=c, bulk_velocity=v, box=box))
+    hot = subs[6]  # particles far too fast for their own mass: it disrupts
+    hot["vel"] = ((hot["vel"] - centres[6][1]) * 40.0 + centres[6][1]).astype(np.float32)
+    S._assign_ids(rng, subs)
+    b = S.concat(subs)
+    nests = [[] for _ in specs]
+    for k, sp in enumerate(specs):
+        if sp[2] is not None:
+            nests[sp[2]].append(k)
+    nest_off = np.concatenate([[0], np.cumsum([len(x) for x in nests])]).astype(np.int64)
+    nest_idx = np.array([c for x in nests for c in x], np.int64)
+    forest = dict(id=b["id"], pos=b["pos"], vel=b["vel"], mass=b["mass"], type=b["type"],
+                  list_off=b["offsets"], nbound_prev=np.array([sp[5] for sp in specs], np.int64),
+                  nest_off=nest_off, nest_idx=nest_idx, roots=np.array([0, 7, 9], np.int64),
+                  ref_pos=b["ref_pos"], ref_vel=b["ref_vel"], mostbound_pos=b["mostbound_pos"],
+                  mostbound_vel=b["mostbound_vel"], mostbound_id=b["mostbound_id"])
+    return forest
+
+
+def forest_cases(ref):
+    p = S.default_params()
+    forest = forest_case()
+    off, pos, res = ref.recursive_unbind(p, forest, relax=3.0)
+    np.savez_compressed(os.path.join(HERE, "forest_10.npz"),
+                        **{f"in_{k}": np.asarray(v) for k, v in forest.items()},
+                        **{f"par_{k}": np.asarray(v) for k, v in p.items()},
+                        relax=np.float64(3.0), ref_off=off, ref_pos_out=pos,
+                        **{f"ref_{k}": np.array([r[k] for r in res]) for k in RESULT_KEYS})
+    print(f"forest_10: {int(forest['list_off'][-1])} particles, final lists {int(off[-1])}, "
+          f"nbound {[int(r['nbound']) for r in res]}")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["index"]:
         index_cases(Oracle(reference=True))
+    elif sys.argv[1:] == ["forest"]:
+        forest_cases(Oracle(reference=True))
     else:
         main()
         index_cases(Oracle(reference=True))
+        forest_cases(Oracle(reference=True))

@@ -8,7 +8,7 @@ import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 SINGLE_CASES = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                      if not os.path.basename(f).startswith(("first_pass", "batch", "index")))
+                      if not os.path.basename(f).startswith(("first_pass", "batch", "index", "forest")))
 FIRST_PASS_CASES = sorted(os.path.basename(f)[:-4]
                           for f in glob.glob(os.path.join(GOLDEN, "first_pass_*.npz")))
 
@@ -81,3 +81,50 @@ def partition_emulation(E: np.ndarray):
             src[pos[kk - 1]] = neg[kk]
     src[vd] = 0
     return int(vd + (E[0] < 0)), src
+
+
+def recursive_unbind_oracle(orc, params, forest, relax=3.0):
+    """RecursiveUnbind + TruncateSource restated literally (depth first, one
+    subhalo at a time; src/subhalo_unbind.cpp:432-458) on the C oracle's Unbind.
+    Returns (final list offsets, positions into the input rows, nbound)."""
+    lo = np.asarray(forest["list_off"], np.int64)
+    no = np.asarray(forest["nest_off"], np.int64)
+    ni = np.asarray(forest["nest_idx"], np.int64)
+    nsub = len(lo) - 1
+    final = [np.arange(lo[s], lo[s + 1]) for s in range(nsub)]
+    nbound = np.asarray(forest["nbound_prev"], np.int64).copy()
+
+    def unbind(s, rows):
+        sub = {k: np.asarray(forest[k])[rows] for k in ("id", "pos", "vel", "mass", "type")}
+        for k in ("ref_pos", "ref_vel", "mostbound_pos", "mostbound_vel"):
+            sub[k] = np.asarray(forest[k])[s]
+        sub["mostbound_id"] = int(forest["mostbound_id"][s])
+        order, _, res = orc.unbind(params, sub)
+        return rows[order], int(res["nbound"])
+
+    def rec(s):
+        orphan = nbound[s] <= 1
+        rows = np.arange(lo[s], lo[s + 1])
+        backup = rows.copy() if orphan else None
+        for c in ni[no[s]:no[s + 1]]:
+            rec(int(c))
+            rows = np.concatenate([rows, final[c][nbound[c]:]])
+        if orphan:
+            rows, backup = backup, rows
+        rows, nbound[s] = unbind(s, rows)
+        if orphan:
+            rows, backup = backup, rows
+        final[s] = rows
+
+    for r in forest["roots"]:
+        rec(int(r))
+    off, out = [0], []
+    for s in range(nsub):
+        if nbound[s] <= 1:
+            ns = nbound[s]
+        else:
+            ns = int(np.float32(nbound[s]) * np.float32(relax))
+        ns = min(ns, len(final[s]))
+        out.append(final[s][:ns])
+        off.append(off[-1] + ns)
+    return np.array(off, np.int64), np.concatenate(out), nbound
