@@ -70,6 +70,16 @@ class hbtu_particles(C.Structure):
     ]
 
 
+class hbtu_props(C.Structure):
+    _fields_ = [
+        ("rmax_comoving", C.c_float), ("vmax_physical", C.c_float),
+        ("last_max_vmax_physical", C.c_float), ("snapshot_of_last_max_vmax", C.c_int32),
+        ("r2sigma_comoving", C.c_float), ("rhalf_comoving", C.c_float),
+        ("r200crit_comoving", C.c_float), ("m200crit", C.c_float),
+        ("inertial_tensor", C.c_float * 6), ("inertial_tensor_weighted", C.c_float * 6),
+    ]
+
+
 class hbtu_stats(C.Structure):
     _fields_ = [
         ("total_ms", C.c_double), ("tree_ms", C.c_double), ("walk_ms", C.c_double),
@@ -107,6 +117,9 @@ SIGNATURES = {
     "hbtu_unbind_noalloc": (C.c_int, [C.POINTER(hbtu_params), C.POINTER(hbtu_particles), C.c_int64,
                                       C.POINTER(hbtu_state), C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p]),
+    "hbtu_subhalo_properties": (C.c_int, [C.c_void_p, C.POINTER(hbtu_particles), C.c_int64,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_int32, C.c_void_p]),
     "hbtu_index_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "hbtu_index_destroy": (C.c_int, [C.c_void_p]),
     "hbtu_index_fill": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,

@@ -145,6 +145,31 @@ def result_to_dict(r: _lib.hbtu_result) -> dict:
     return out
 
 
+def results_array(results) -> C.Array:
+    """Inverse of result_to_dict over a list: a ctypes hbtu_result array."""
+    arr = (_lib.hbtu_result * max(len(results), 1))()
+    for s, d in enumerate(results):
+        for name, _ in _lib.hbtu_result._fields_:
+            if name not in d:
+                continue
+            v = d[name]
+            if hasattr(v, "__len__"):
+                dst = getattr(arr[s], name)
+                for k in range(len(v)):
+                    dst[k] = v[k]
+            else:
+                setattr(arr[s], name, v.item() if hasattr(v, "item") else v)
+    return arr
+
+
+def props_to_dict(p: _lib.hbtu_props) -> dict:
+    out = {}
+    for name, _ in _lib.hbtu_props._fields_:
+        v = getattr(p, name)
+        out[name] = np.array(list(v), np.float32) if hasattr(v, "__len__") else v
+    return out
+
+
 def _state(ref_pos, ref_vel, mb_pos, mb_vel, mb_id) -> _lib.hbtu_state:
     s = _lib.hbtu_state()
     for k in range(3):
@@ -314,6 +339,55 @@ class Unbinder:
                                         C.addressof(states), out["order"].data_ptr(),
                                         out["energy"].data_ptr(), out["res"].data_ptr())
         _lib.check(rc, self.handle)
+
+    # -- properties of the bound part (Subhalo_t::CalculateProfileProperties,
+    #    ::CalculateShape, src/subhalo.cpp:242-398) ----------------------------
+    def subhalo_properties(self, batch: dict, order, results, last_max_vmax=None,
+                           last_snap=None, snapshot_index: int = 0):
+        """Properties of every subhalo of a batch that unbind_batch has just
+        unbound (host arrays): ``order`` and ``results`` as it returned them,
+        ``last_max_vmax`` / ``last_snap`` per subhalo before this snapshot.
+        Returns one dict per subhalo (hbtu_props fields)."""
+        off = np.ascontiguousarray(batch["offsets"], np.int64)
+        nsub = len(off) - 1
+        d = dict(batch)
+        d.setdefault("vel", np.zeros((int(off[-1]), 3), np.float32))
+        d.setdefault("id", np.zeros(int(off[-1]), np.int64))
+        p, keep = self._host_particles(d)
+        ordr = np.ascontiguousarray(order, np.int64)
+        res = results_array(results)
+        lm = None if last_max_vmax is None else np.ascontiguousarray(last_max_vmax, np.float32)
+        ls = None if last_snap is None else np.ascontiguousarray(last_snap, np.int32)
+        out = (_lib.hbtu_props * max(nsub, 1))()
+        rc = self.lib.hbtu_subhalo_properties(self.handle, C.byref(p), nsub, _ptr(off),
+                                              _ptr(ordr), C.addressof(res),
+                                              _ptr(lm) if lm is not None else 0,
+                                              _ptr(ls) if ls is not None else 0,
+                                              int(snapshot_index), C.addressof(out))
+        _lib.check(rc, self.handle)
+        del keep
+        return [props_to_dict(out[s]) for s in range(nsub)]
+
+    def subhalo_properties_device(self, dev: dict, offsets: np.ndarray, order, res,
+                                  last_max_vmax=None, last_snap=None, snapshot_index: int = 0):
+        """subhalo_properties on device-resident torch tensors: ``dev`` holds
+        pos and mass, ``order`` and ``res`` are the outputs of
+        unbind_batch_device.  Returns the ctypes hbtu_props array."""
+        off = np.ascontiguousarray(offsets, np.int64)
+        nsub = len(off) - 1
+        p = _lib.hbtu_particles(id=0, pos=dev["pos"].data_ptr(), vel=0,
+                                mass=dev["mass"].data_ptr(), type=0,
+                                location=_lib.HBTU_DEVICE, reserved=0)
+        lm = None if last_max_vmax is None else np.ascontiguousarray(last_max_vmax, np.float32)
+        ls = None if last_snap is None else np.ascontiguousarray(last_snap, np.int32)
+        out = (_lib.hbtu_props * max(nsub, 1))()
+        rc = self.lib.hbtu_subhalo_properties(self.handle, C.byref(p), nsub, _ptr(off),
+                                              order.data_ptr(), res.data_ptr(),
+                                              _ptr(lm) if lm is not None else 0,
+                                              _ptr(ls) if ls is not None else 0,
+                                              int(snapshot_index), C.addressof(out))
+        _lib.check(rc, self.handle)
+        return out
 
     @staticmethod
     def make_states(batch: dict):

@@ -235,6 +235,45 @@ hbtu_status hbtu_energy_gradient(hbtu_handle *h, const hbtu_particles *p, int64_
 hbtu_status hbtu_direct_potential(hbtu_handle *h, const hbtu_particles *p, int64_t n,
                                   const int64_t *targets, int64_t ntarget, double *potential_out);
 
+/* Post-unbinding properties of a subhalo: the members of Subhalo_t written
+ * by CalculateProfileProperties (src/subhalo.cpp:242-335) and CalculateShape
+ * (src/subhalo.cpp:337-398). */
+typedef struct hbtu_props {
+  float rmax_comoving;              /* RmaxComoving */
+  float vmax_physical;              /* VmaxPhysical */
+  float last_max_vmax_physical;     /* LastMaxVmaxPhysical (updated) */
+  int32_t snapshot_of_last_max_vmax; /* SnapshotIndexOfLastMaxVmax (updated) */
+  float r2sigma_comoving;           /* R2SigmaComoving */
+  float rhalf_comoving;             /* RHalfComoving */
+  float r200crit_comoving;          /* BoundR200CritComoving */
+  float m200crit;                   /* BoundM200Crit */
+  float inertial_tensor[6];         /* InertialTensor {xx, xy, xz, yy, yz, zz} */
+  float inertial_tensor_weighted[6]; /* InertialTensorWeighted */
+} hbtu_props;
+
+/* CalculateProfileProperties + CalculateShape of every subhalo of a batch
+ * that hbtu_unbind_batch (or hbtu_unbind, nsub = 1) has just unbound, on the
+ * first nbound particles of each subhalo's output order.
+ *   p, nsub, offsets: the particles and offsets given to the unbinding
+ *     (offsets in host memory; pos and mass are read);
+ *   order, res: its order_out and res, in the memory p->location names;
+ *   last_max_vmax, last_snap: nsub values of LastMaxVmaxPhysical and
+ *     SnapshotIndexOfLastMaxVmax before the call (host memory; NULL: 0 and -1);
+ *   snapshot_index: the epoch's snapshot index (Snapshot_t::GetSnapshotIndex);
+ *   out: nsub records (host memory).
+ * G, Hz and the scale factor come from the handle's parameters; the
+ * overdensity is 200 times critical (Snapshot_t::HaloVirialFactors,
+ * src/snapshot.cpp:328-336).  A subhalo with nbound <= 1 gets zeros and its
+ * last-maximum fields unchanged, as in the reference.  Distance ties keep the
+ * unbinding order; the inertia tensors may differ from the reference's
+ * sequential sums by one unit in the last place (the order of the double
+ * sum); every other field is exact. */
+hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_particles *p, int64_t nsub,
+                                    const int64_t *offsets, const int64_t *order,
+                                    const hbtu_result *res, const float *last_max_vmax,
+                                    const int32_t *last_snap, int32_t snapshot_index,
+                                    hbtu_props *out);
+
 /* Particle-ID -> index tables, the ID re-resolve of the unbinding step's
  * callers (IndexTable_t, src/hash.h:47-112; filled from a snapshot's IDs by
  * ParticleSnapshot_t, src/snapshot.h:191-224, and queried by GetIndex /

@@ -922,3 +922,109 @@ int hbto_index_lookup(int flat, const int64_t *keys, const int64_t *values, int6
     mapped_lookup(keys, values, n, null_index, queries, m, out);
   return 0;
 }
+
+/* ------------------------------------------------------------ properties */
+
+typedef struct {
+  float r, m, v;
+  int64_t k;
+} radmass;
+
+static int cmp_radmass(const void *a, const void *b)
+{
+  const radmass *x = (const radmass *)a, *y = (const radmass *)b;
+  if (x->r != y->r) return x->r < y->r ? -1 : 1;
+  return x->k < y->k ? -1 : (x->k > y->k); /* ties keep the given order */
+}
+
+int hbto_subhalo_properties(const hbto_params *par, int64_t nbound, const float *pos,
+                            const float *mass, const float cen[3], float mbound,
+                            float last_max_vmax, int32_t last_snap, int32_t snapshot_index,
+                            hbto_props *out)
+{
+  dpar d;
+  derive(par, &d);
+  memset(out, 0, sizeof(*out));
+  out->last_max_vmax_physical = last_max_vmax;
+  out->snapshot_of_last_max_vmax = last_snap;
+  if (nbound <= 1) return 0; /* subhalo.cpp:264-282, :339-351 */
+  const float G = (float)par->G, a = (float)par->scale_factor, Hz = (float)par->hubble;
+  const float eps = (float)par->softening;
+  /* CalculateProfileProperties (subhalo.cpp:283-312): distances to the most-bound
+   * particle (PeriodicDistance, config_parser.h:143-156), sorted, cumulative mass
+   * in double, radius floored at the softening, v^2 = m / r */
+  const float VelocityUnit = G / a;
+  radmass *prof = malloc((size_t)nbound * sizeof(radmass));
+  for (int64_t i = 0; i < nbound; i++) {
+    float dx[3];
+    for (int j = 0; j < 3; j++) {
+      dx[j] = pos[3 * i + j] - cen[j];
+      if (d.periodic) dx[j] = nearest_f(dx[j], &d);
+    }
+    prof[i].r = sqrtf(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+    prof[i].m = mass[i];
+    prof[i].k = i;
+  }
+  qsort(prof, (size_t)nbound, sizeof(radmass), cmp_radmass);
+  double m_cum = 0.;
+  for (int64_t i = 0; i < nbound; i++) prof[i].m = (float)(m_cum += prof[i].m);
+  for (int64_t i = 0; i < nbound; i++) {
+    if (prof[i].r < eps) prof[i].r = eps;
+    prof[i].v = prof[i].m / prof[i].r;
+  }
+  int64_t imax = 0;
+  for (int64_t i = 1; i < nbound; i++)
+    if (prof[i].v > prof[imax].v) imax = i; /* max_element: the first maximum */
+  out->rmax_comoving = prof[imax].r;
+  out->vmax_physical = sqrtf(prof[imax].v * VelocityUnit);
+  out->rhalf_comoving = prof[nbound / 2].r;
+  out->r2sigma_comoving = prof[(int64_t)(nbound * 0.955)].r;
+  /* SphericalOverdensitySize with virialF_c200 = 200 (snapshot.cpp:259-281, :328-336) */
+  const float RhoVirial = (float)((double)(200.f * Hz * Hz) / 2.0 / (double)G * (double)a *
+                                  (double)a * (double)a);
+  for (int64_t i = nbound - 1; i >= 0; i--) {
+    const float r = prof[i].r, m = prof[i].m;
+    if (m > RhoVirial * r * r * r) {
+      out->m200crit = m;
+      out->r200crit_comoving = (float)pow((double)(m / RhoVirial), 1.0 / 3);
+      break;
+    }
+  }
+  if (out->vmax_physical >= last_max_vmax) { /* subhalo.cpp:314-318 */
+    out->snapshot_of_last_max_vmax = snapshot_index;
+    out->last_max_vmax_physical = out->vmax_physical;
+  }
+  free(prof);
+  /* CalculateShape (subhalo.cpp:352-392): float terms summed in double over the
+   * bound particles after the most-bound one */
+  double I[6] = {0, 0, 0, 0, 0, 0}, W[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t i = 1; i < nbound; i++) {
+    const float m = mass[i];
+    float dx = pos[3 * i] - cen[0], dy = pos[3 * i + 1] - cen[1], dz = pos[3 * i + 2] - cen[2];
+    if (d.periodic) {
+      dx = nearest_f(dx, &d);
+      dy = nearest_f(dy, &d);
+      dz = nearest_f(dz, &d);
+    }
+    const float dx2 = dx * dx, dy2 = dy * dy, dz2 = dz * dz;
+    I[0] += dx2 * m;
+    I[3] += dy2 * m;
+    I[5] += dz2 * m;
+    I[1] += dx * dy * m;
+    I[2] += dx * dz * m;
+    I[4] += dy * dz * m;
+    float dr2 = dx2 + dy2 + dz2;
+    dr2 /= m;
+    W[0] += dx2 / dr2;
+    W[3] += dy2 / dr2;
+    W[5] += dz2 / dr2;
+    W[1] += dx * dy / dr2;
+    W[2] += dx * dz / dr2;
+    W[4] += dy * dz / dr2;
+  }
+  for (int k = 0; k < 6; k++) {
+    out->inertial_tensor[k] = (float)I[k] / mbound;
+    out->inertial_tensor_weighted[k] = (float)W[k] / mbound;
+  }
+  return 0;
+}

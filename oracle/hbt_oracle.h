@@ -118,6 +118,26 @@ void hbto_srand48(long seed);
  * (src/subhalo_unbind.cpp:302): perm[i] = original index now at i. */
 void hbto_reference_shuffle(int64_t n, unsigned seed, int64_t *perm);
 
+/* Post-unbinding properties of a subhalo (Subhalo_t members written by
+ * CalculateProfileProperties, src/subhalo.cpp:242-335, and CalculateShape,
+ * :337-398). */
+typedef struct {
+  float rmax_comoving, vmax_physical, last_max_vmax_physical;
+  int32_t snapshot_of_last_max_vmax;
+  float r2sigma_comoving, rhalf_comoving, r200crit_comoving, m200crit;
+  float inertial_tensor[6], inertial_tensor_weighted[6];
+} hbto_props;
+
+/* CalculateProfileProperties + CalculateShape (src/subhalo.cpp:242-398) of a
+ * subhalo whose bound particles, most-bound first, are pos[3*nbound] and
+ * mass[nbound]; cen is ComovingMostBoundPosition, mbound its Mbound; the
+ * epoch is snapshot `snapshot_index` with G, Hz, a from par.  Ties in radius
+ * keep the given order (the reference's std::sort leaves them unspecified). */
+int hbto_subhalo_properties(const hbto_params *par, int64_t nbound, const float *pos,
+                            const float *mass, const float cen[3], float mbound,
+                            float last_max_vmax, int32_t last_snap, int32_t snapshot_index,
+                            hbto_props *out);
+
 /* Particle-ID -> index tables (src/hash.h:47-112, src/hash.tpp, src/hash_remote.tpp).
  * Fill a table with the pairs (keys[i], values[i]), i < n (KeyList_t::GetKey and
  * ::GetIndex), then look up every query: out[j] = GetIndex(queries[j]), or

@@ -69,6 +69,24 @@ class Result(C.Structure):
     ]
 
 
+class Props(C.Structure):
+    _fields_ = [
+        ("rmax_comoving", C.c_float), ("vmax_physical", C.c_float),
+        ("last_max_vmax_physical", C.c_float), ("snapshot_of_last_max_vmax", C.c_int32),
+        ("r2sigma_comoving", C.c_float), ("rhalf_comoving", C.c_float),
+        ("r200crit_comoving", C.c_float), ("m200crit", C.c_float),
+        ("inertial_tensor", C.c_float * 6), ("inertial_tensor_weighted", C.c_float * 6),
+    ]
+
+
+def props_dict(p: Props) -> dict:
+    out = {}
+    for name, _ in Props._fields_:
+        v = getattr(p, name)
+        out[name] = np.array(list(v), np.float32) if hasattr(v, "__len__") else v
+    return out
+
+
 def result_dict(r: Result) -> dict:
     out = {}
     for name, _ in Result._fields_:
@@ -159,6 +177,54 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"index lookup failed ({rc})")
         return out[:len(q)]
+
+    def unbind_properties(self, params: dict, sub: dict, last_max_vmax: float = 0.0,
+                          last_snap: int = -1):
+        """The reference's Unbind followed by CalculateProfileProperties and
+        CalculateShape (reference build only; the epoch is snapshot 1)."""
+        if not self.reference:
+            raise ValueError("exists in the reference build only")
+        n = len(sub["mass"])
+        ids = np.ascontiguousarray(sub["id"], np.int64)
+        pos = np.ascontiguousarray(sub["pos"], np.float32).reshape(-1)
+        vel = np.ascontiguousarray(sub["vel"], np.float32).reshape(-1)
+        mass = np.ascontiguousarray(sub["mass"], np.float32)
+        typ = np.ascontiguousarray(sub.get("type", np.ones(n, np.int32)), np.int32)
+        st = State()
+        for j in range(3):
+            st.ref_pos[j] = float(sub["ref_pos"][j])
+            st.ref_vel[j] = float(sub["ref_vel"][j])
+            st.mostbound_pos[j] = float(sub["mostbound_pos"][j])
+            st.mostbound_vel[j] = float(sub["mostbound_vel"][j])
+        st.mostbound_id = int(sub.get("mostbound_id", ids[0] if n else -1))
+        order = np.zeros(max(n, 1), np.int64)
+        energy = np.zeros(max(n, 1), np.float32)
+        res, props = Result(), Props()
+        fn = self.lib.ref_unbind_properties
+        fn.restype = C.c_int
+        rc = fn(C.byref(make_params(params)), C.c_int64(n), _p(ids, C.c_int64), _p(pos, C.c_float),
+                _p(vel, C.c_float), _p(mass, C.c_float), _p(typ, C.c_int32), C.byref(st),
+                C.c_float(last_max_vmax), C.c_int32(last_snap), _p(order, C.c_int64),
+                _p(energy, C.c_float), C.byref(res), C.byref(props))
+        if rc != 0:
+            raise RuntimeError("ref_unbind_properties failed")
+        return order[:n], result_dict(res), props_dict(props)
+
+    def subhalo_properties(self, params: dict, pos, mass, cen, mbound: float,
+                           last_max_vmax: float = 0.0, last_snap: int = -1,
+                           snapshot_index: int = 1) -> dict:
+        """The C restatement of CalculateProfileProperties + CalculateShape on
+        a subhalo's bound particles (most-bound first)."""
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1)
+        mass = np.ascontiguousarray(mass, np.float32)
+        c = (C.c_float * 3)(*[float(x) for x in cen])
+        props = Props()
+        fn = self.lib.hbto_subhalo_properties
+        fn.restype = C.c_int
+        fn(C.byref(make_params(params)), C.c_int64(len(mass)), _p(pos, C.c_float),
+           _p(mass, C.c_float), c, C.c_float(mbound), C.c_float(last_max_vmax),
+           C.c_int32(last_snap), C.c_int32(snapshot_index), C.byref(props))
+        return props_dict(props)
 
     def recursive_unbind(self, params: dict, forest: dict, relax: float = 3.0):
         """The reference's RecursiveUnbind over a forest, then TruncateSource

@@ -236,6 +236,48 @@ int ref_recursive_unbind(const hbto_params *par, double relax_factor, int64_t ns
   return 0;
 }
 
+/* Unbind, then the reference's CalculateProfileProperties and CalculateShape
+ * (src/subhalo.cpp:242-398) on the result; last_max_vmax and last_snap are
+ * the subhalo's LastMaxVmaxPhysical and SnapshotIndexOfLastMaxVmax before the
+ * call (the epoch is snapshot 1). */
+int ref_unbind_properties(const hbto_params *par, int64_t n, const int64_t *id, const float *pos,
+                          const float *vel, const float *mass, const int32_t *type,
+                          const hbto_state *st, float last_max_vmax, int32_t last_snap,
+                          int64_t *order, float *energy, hbto_result *res, hbto_props *props)
+{
+  setup(par);
+  omp_set_num_threads(1);
+  omp_set_max_active_levels(1);
+  PhysicalConst::H0 = 100.;
+  Epoch_t epoch(par);
+  Subhalo_t sub;
+  fill_subhalo(sub, n, id, pos, vel, mass, type, st);
+  sub.LastMaxVmaxPhysical = last_max_vmax;
+  sub.SnapshotIndexOfLastMaxVmax = last_snap;
+  sub.BoundM200Crit = 0.f;  // left as is when no radius qualifies (snapshot.cpp:270-280)
+  sub.BoundR200CritComoving = 0.f;
+  srand(0);
+  sub.Unbind(epoch);
+  sub.CalculateProfileProperties(epoch);
+  sub.CalculateShape();
+  std::vector<int64_t> ids, ipos;
+  sorted_ids(n, id, ids, ipos);
+  read_subhalo(sub, n, ipos.data(), ids.data(), order, energy, res, n);
+  props->rmax_comoving = sub.RmaxComoving;
+  props->vmax_physical = sub.VmaxPhysical;
+  props->last_max_vmax_physical = sub.LastMaxVmaxPhysical;
+  props->snapshot_of_last_max_vmax = sub.SnapshotIndexOfLastMaxVmax;
+  props->r2sigma_comoving = sub.R2SigmaComoving;
+  props->rhalf_comoving = sub.RHalfComoving;
+  props->r200crit_comoving = sub.BoundR200CritComoving;
+  props->m200crit = sub.BoundM200Crit;
+  for (int k = 0; k < 6; k++) {
+    props->inertial_tensor[k] = sub.InertialTensor[k];
+    props->inertial_tensor_weighted[k] = sub.InertialTensorWeighted[k];
+  }
+  return 0;
+}
+
 /* The reference's own tables: Fill, then GetIndex per query (src/hash.tpp). */
 int ref_index_lookup(int flat, const int64_t *keys, const int64_t *values, int64_t n,
                      int64_t null_index, const int64_t *queries, int64_t m, int64_t *out)

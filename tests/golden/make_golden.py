@@ -204,12 +204,80 @@ def forest_cases(ref):
           f"nbound {[int(r['nbound']) for r in res]}")
 
 
+PROPS_KEYS = ("rmax_comoving", "vmax_physical", "last_max_vmax_physical",
+              "snapshot_of_last_max_vmax", "r2sigma_comoving", "rhalf_comoving",
+              "r200crit_comoving", "m200crit", "inertial_tensor", "inertial_tensor_weighted")
+
+
+def wide_masses(sub, seed, octaves):
+    """Particle masses spread over 2^-octaves .. 2^octaves times the base mass,
+    with random mantissas (mixed species)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    f = np.exp2(rng.uniform(-octaves, octaves, len(sub["mass"])))
+    sub["mass"] = (sub["mass"].astype(np.float64) * f).astype(np.float32)
+    return sub
+
+
+def props_batch(name, params, specs, ref):
+    """Each subhalo unbound by the reference's Unbind, then its
+    CalculateProfileProperties and CalculateShape (epoch: snapshot 1), stored
+    as one batch: inputs, order, results and properties per subhalo."""
+    subs, orders, results, props = [], [], [], []
+    for sub, lm, ls in specs:
+        o, r, pr = ref.unbind_properties(params, sub, last_max_vmax=lm, last_snap=ls)
+        subs.append(sub)
+        orders.append(o)
+        results.append(r)
+        props.append(pr)
+    off = np.concatenate([[0], np.cumsum([len(s["mass"]) for s in subs])]).astype(np.int64)
+    cat = {k: np.concatenate([s[k] for s in subs]) for k in ("id", "pos", "vel", "mass", "type")}
+    per = {k: np.array([s[k] for s in subs]) for k in ("ref_pos", "ref_vel", "mostbound_pos",
+                                                       "mostbound_vel")}
+    per["mostbound_id"] = np.array([int(s.get("mostbound_id", s["id"][0])) for s in subs])
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"),
+        **{f"in_{k}": v for k, v in cat.items()}, **{f"in_{k}": v for k, v in per.items()},
+        in_offsets=off, in_last_max_vmax=np.array([s[1] for s in specs], np.float32),
+        in_last_snap=np.array([s[2] for s in specs], np.int32), snapshot_index=np.int32(1),
+        **{f"par_{k}": np.asarray(v) for k, v in params.items()},
+        ref_order=np.concatenate(orders),
+        **{f"ref_{k}": np.array([r[k] for r in results]) for k in RESULT_KEYS},
+        **{f"props_{k}": np.array([q[k] for q in props]) for k in PROPS_KEYS})
+    print(f"{name}: {len(subs)} subhaloes, nbound {[int(r['nbound']) for r in results]}")
+
+
+def props_cases(ref):
+    p = S.default_params()
+    hot = scaled(300, 127)
+    hot["vel"] = (hot["vel"] * 40.0).astype(np.float32)
+    props_batch("props_10", p, [
+        (scaled(3000, 121), 0.0, -1),
+        (scaled(1000, 122, c=15.0, center=(0.01, 99.99, 50.0)), 0.0, -1),  # periodic corner
+        (scaled(20000, 123, c=8.0), 0.0, -1),
+        (scaled(50, 124, cf=0.0), 0.0, -1),
+        (scaled(3, 125, cf=0.0), 0.0, -1),
+        (scaled(2000, 126), 1e9, 0),       # below the last maximum: kept
+        (scaled(2000, 126), 150.0, 0),     # the same subhalo above a lower last maximum
+        (hot, 7.0, 0),                      # disrupted: nothing computed, last maximum kept
+        (wide_masses(scaled(20000, 128), 129, 8.0), 0.0, -1),   # mixed species
+        (wide_masses(scaled(4000, 130), 131, 30.0), 0.0, -1),   # masses over 2^60
+    ], ref)
+    pa = S.default_params(scale_factor=0.5, hubble=180.0, periodic=0)
+    props_batch("props_a05", pa, [
+        (scaled(5000, 132, center=(30.0, 40.0, 50.0)), 0.0, -1),
+        (scaled(800, 133, c=4.0, center=(60.0, 40.0, 50.0)), 12.0, 0),
+    ], ref)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["index"]:
         index_cases(Oracle(reference=True))
     elif sys.argv[1:] == ["forest"]:
         forest_cases(Oracle(reference=True))
+    elif sys.argv[1:] == ["props"]:
+        props_cases(Oracle(reference=True))
     else:
         main()
         index_cases(Oracle(reference=True))
         forest_cases(Oracle(reference=True))
+        props_cases(Oracle(reference=True))
