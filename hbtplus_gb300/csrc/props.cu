@@ -43,14 +43,25 @@ struct PropSeg {
   int64_t off;   // first particle of the subhalo in the batch
   int64_t boff;  // first bound element in the flat bound index space
   int64_t nb;    // Nbound (0 when <= 1: no properties)
+  int64_t n;     // particles of the subhalo
   float cen[3];  // ComovingMostBoundPosition
   float mbound;
   int chunk0, nchunk;  // shape chunks
 };
 
 // Flags of one call (device): [0] sort look-back error, [1] lowest set bit of
-// any mass (power of two), [2] highest, [3] a negative or non-finite mass.
-enum { F_SORT = 0, F_LOW = 1, F_HIGH = 2, F_NEG = 3, F_WORDS = 4 };
+// any mass (power of two), [2] highest, [3] a negative or non-finite mass,
+// [4] an order entry outside its subhalo.
+enum { F_SORT = 0, F_LOW = 1, F_HIGH = 2, F_NEG = 3, F_ORDER = 4, F_WORDS = 5 };
+
+// Particle at bound position k of subhalo g (an order entry outside the
+// subhalo reads its first particle; k_pr_elem reports it).
+__device__ __forceinline__ int64_t bound_particle(const PropSeg &g, const int64_t *order,
+                                                  int64_t k, int64_t n)
+{
+  const int64_t o = order[g.off + k];
+  return g.off + ((o >= 0 && o < n) ? o : 0);
+}
 
 __device__ __forceinline__ int seg_of(const int64_t *boff, int S, int64_t j)
 {
@@ -101,7 +112,9 @@ __global__ void __launch_bounds__(kPB) k_pr_elem(const PropSeg *seg, const int64
   if (j >= T) return;
   const int s = seg_of(boff, S, j);
   const PropSeg g = seg[s];
-  const int64_t pid = g.off + order[g.off + (j - g.boff)];
+  const int64_t o = order[g.off + (j - g.boff)];
+  if (o < 0 || o >= g.n) atomicOr(&flags[F_ORDER], 1);
+  const int64_t pid = bound_particle(g, order, j - g.boff, g.n);
   const float x[3] = {pos[3 * pid], pos[3 * pid + 1], pos[3 * pid + 2]};
   const float r = periodic_distance(x, g.cen, P);
   lo[j] = (unsigned long long)__float_as_uint(r);  // r >= 0: bits sort as values
@@ -134,7 +147,7 @@ __global__ void __launch_bounds__(kPB) k_pr_fix(const PropSeg *seg, const int64_
   const int64_t j = val[q];
   const int s = seg_of(boff, S, j);
   const PropSeg g = seg[s];
-  const float m = mass[g.off + order[g.off + (j - g.boff)]];
+  const float m = mass[bound_particle(g, order, j - g.boff, g.n)];
   msorted[q] = m;
   int K;
   mfix[q] = fix_scale(flags, T, &K) ? (long long)ldexp((double)m, K) : 0;  // exact: below 2^62
@@ -213,7 +226,7 @@ __global__ void __launch_bounds__(kPB) k_pr_shape(const PropSeg *seg, const int 
   double v[12];
   for (int k = 0; k < 12; k++) v[k] = 0.;
   for (int64_t i = lo + threadIdx.x; i < hi; i += kPB) {
-    const int64_t pid = g.off + order[g.off + i];
+    const int64_t pid = bound_particle(g, order, i, g.n);
     const float m = mass[pid];
     float dx = fsub(pos[3 * pid], g.cen[0]), dy = fsub(pos[3 * pid + 1], g.cen[1]),
           dz = fsub(pos[3 * pid + 2], g.cen[2]);
@@ -357,6 +370,7 @@ extern "C" hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_partic
       PropSeg &g = seg[s];
       g.off = offsets[s];
       const int64_t n = offsets[s + 1] - offsets[s];
+      g.n = n;
       g.nb = R[s].nbound > 1 ? std::min<int64_t>(R[s].nbound, n) : 0;
       g.boff = T;
       boff[s] = T;
@@ -443,7 +457,7 @@ extern "C" hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_partic
       HBTU_CUDA(cudaMemcpyAsync(d_last, last_max_vmax, 4 * nsub, cudaMemcpyHostToDevice, st));
     if (d_lsnap)
       HBTU_CUDA(cudaMemcpyAsync(d_lsnap, last_snap, 4 * nsub, cudaMemcpyHostToDevice, st));
-    const int init_flags[F_WORDS] = {0, 0x7fffffff, -0x7fffffff, 0};
+    const int init_flags[F_WORDS] = {0, 0x7fffffff, -0x7fffffff, 0, 0};
     HBTU_CUDA(cudaMemcpyAsync(d_flags, init_flags, sizeof(init_flags), cudaMemcpyHostToDevice, st));
     HBTU_CUDA(cudaMemsetAsync(d_vmax, 0, 8 * nsub, st));
     HBTU_CUDA(cudaMemsetAsync(d_so, 0xff, 8 * nsub, st));  // -1: no radius qualifies
@@ -494,6 +508,10 @@ extern "C" hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_partic
     if (hflags[F_SORT]) {
       h->err = "subhalo properties: radix sort look-back wait ran out";
       return HBTU_ERR_CUDA;
+    }
+    if (hflags[F_ORDER]) {
+      h->err = "subhalo properties: an order entry lies outside its subhalo";
+      return HBTU_ERR_INVALID_ARGUMENT;
     }
     // BoundR200CritComoving = pow(M200Crit / RhoVirial, 1/3) in double (snapshot.cpp:277)
     for (int64_t s = 0; s < nsub; s++)

@@ -181,7 +181,8 @@ class Oracle:
     def unbind_properties(self, params: dict, sub: dict, last_max_vmax: float = 0.0,
                           last_snap: int = -1):
         """The reference's Unbind followed by CalculateProfileProperties and
-        CalculateShape (reference build only; the epoch is snapshot 1)."""
+        CalculateShape (reference build only; the epoch is snapshot 1):
+        (order, energy, result, properties)."""
         if not self.reference:
             raise ValueError("exists in the reference build only")
         n = len(sub["mass"])
@@ -208,7 +209,7 @@ class Oracle:
                 _p(energy, C.c_float), C.byref(res), C.byref(props))
         if rc != 0:
             raise RuntimeError("ref_unbind_properties failed")
-        return order[:n], result_dict(res), props_dict(props)
+        return order[:n], energy[:n], result_dict(res), props_dict(props)
 
     def subhalo_properties(self, params: dict, pos, mass, cen, mbound: float,
                            last_max_vmax: float = 0.0, last_snap: int = -1,

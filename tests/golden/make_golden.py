@@ -12,7 +12,8 @@ the reference tree's BindingEnergy/EvaluatePotential of every particle;
 `index_*` cases hold the reference's particle-ID tables and their lookups
 (`python tests/golden/make_golden.py index` writes only those); `forest_10`
 holds the reference's RecursiveUnbind + TruncateSource over a forest of nested
-subhaloes (`... forest`).
+subhaloes (`... forest`); `props_*` batches hold each subhalo's Unbind followed
+by the reference's CalculateProfileProperties and CalculateShape (`... props`).
 
 For sampled cases the stored particles are the ones AFTER the reference's
 random_shuffle (what the GPU library and the C oracle take), with
@@ -222,11 +223,12 @@ def props_batch(name, params, specs, ref):
     """Each subhalo unbound by the reference's Unbind, then its
     CalculateProfileProperties and CalculateShape (epoch: snapshot 1), stored
     as one batch: inputs, order, results and properties per subhalo."""
-    subs, orders, results, props = [], [], [], []
+    subs, orders, energies, results, props = [], [], [], [], []
     for sub, lm, ls in specs:
-        o, r, pr = ref.unbind_properties(params, sub, last_max_vmax=lm, last_snap=ls)
+        o, e, r, pr = ref.unbind_properties(params, sub, last_max_vmax=lm, last_snap=ls)
         subs.append(sub)
         orders.append(o)
+        energies.append(e)
         results.append(r)
         props.append(pr)
     off = np.concatenate([[0], np.cumsum([len(s["mass"]) for s in subs])]).astype(np.int64)
@@ -240,7 +242,7 @@ def props_batch(name, params, specs, ref):
         in_offsets=off, in_last_max_vmax=np.array([s[1] for s in specs], np.float32),
         in_last_snap=np.array([s[2] for s in specs], np.int32), snapshot_index=np.int32(1),
         **{f"par_{k}": np.asarray(v) for k, v in params.items()},
-        ref_order=np.concatenate(orders),
+        ref_order=np.concatenate(orders), ref_energy=np.concatenate(energies),
         **{f"ref_{k}": np.array([r[k] for r in results]) for k in RESULT_KEYS},
         **{f"props_{k}": np.array([q[k] for q in props]) for k in PROPS_KEYS})
     print(f"{name}: {len(subs)} subhaloes, nbound {[int(r['nbound']) for r in results]}")
