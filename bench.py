@@ -252,8 +252,9 @@ def config_of(args, batch):
 def run_tracking_step(args, ws, rank, local):
     """The tracking step of 20,000 subhaloes (2000-subhalo law) in a 3e7-particle,
     200 Mpc/h snapshot: the snapshot's ID table, the re-resolve of every
-    subhalo's particle IDs after a drift and 10% outer stripping, the gather and
-    the batched unbinding, all on the GPU."""
+    subhalo's particle IDs after a drift and 10% outer stripping, the gather,
+    the batched unbinding and every subhalo's profile and shape, all on the
+    GPU."""
     import torch
 
     from hbtplus_gb300 import _lib
@@ -278,10 +279,12 @@ def run_tracking_step(args, ws, rank, local):
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
 
+    props_args = dict(snapshot_index=1)
+
     def one():
         step.load_snapshot(T["snap_id"], T["snap_pos"], T["snap_vel"], T["snap_mass"],
                            T["snap_type"])
-        return step.run(d["offsets"], T["member_id"], states)
+        return step.run(d["offsets"], T["member_id"], states, properties=props_args)
 
     for _ in range(args.warmup):
         one()
@@ -292,7 +295,7 @@ def run_tracking_step(args, ws, rank, local):
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             flush.fill_(1.0)
-            e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
             e[0].record(stream)
             step.load_snapshot(T["snap_id"], T["snap_pos"], T["snap_vel"], T["snap_mass"],
                                T["snap_type"])
@@ -306,12 +309,16 @@ def run_tracking_step(args, ws, rank, local):
                                        device=dev))
             ub.unbind_batch_device(batch, d["offsets"], states, out)
             e[3].record(stream)
+            ub.subhalo_properties_device(batch, d["offsets"], out["order"], out["res"],
+                                         snapshot_index=1)
+            e[4].record(stream)
             times.append(e)
         torch.cuda.synchronize()
-    ms = [a[0].elapsed_time(a[3]) for a in times]
+    ms = [a[0].elapsed_time(a[4]) for a in times]
     fill_ms = statistics.mean(a[0].elapsed_time(a[1]) for a in times)
     rg_ms = statistics.mean(a[1].elapsed_time(a[2]) for a in times)
     un_ms = statistics.mean(a[2].elapsed_time(a[3]) for a in times)
+    pr_ms = statistics.mean(a[3].elapsed_time(a[4]) for a in times)
     ms_per_step = sum(ms) / args.steps
     st = ub.stats()
     clocks = clk.summary()
@@ -326,20 +333,21 @@ def run_tracking_step(args, ws, rank, local):
         G = {k: v.to(dev, non_blocking=True) for k, v in pin.items()}
         step.load_snapshot(G["snap_id"], G["snap_pos"], G["snap_vel"], G["snap_mass"],
                            G["snap_type"])
-        out, _ = step.run(d["offsets"], G["member_id"], states)
+        out, _ = step.run(d["offsets"], G["member_id"], states, properties=props_args)
         order_host.copy_(out["order"], non_blocking=True)
         res_host.copy_(out["res"], non_blocking=True)
         torch.cuda.synchronize()
         e2e_t.append(time.perf_counter() - t0)
     e2e_s = sum(e2e_t) / args.steps
     h2d = sum(int(v.numel() * v.element_size()) for v in pin.values())
-    d2h = nmem * 8 + nsub * C.sizeof(_lib.hbtu_result)
+    d2h = nmem * 8 + nsub * (C.sizeof(_lib.hbtu_result) + C.sizeof(_lib.hbtu_props))
     # HBM view of the re-resolve + gather phase: per member 8 B id + 8 B index
     # written and read back + 40 B particle read and written
     rg_bytes = nmem * (8 + 8 + 8 + 40 + 40)
     peaks, peak_kind = measured_peaks()
     line = {
-        "metric": "subhalo unbinds/s in a tracking step (ID re-resolve + gather + unbind)",
+        "metric": "subhalo unbinds/s in a tracking step (ID re-resolve + gather + unbind + "
+                  "profile and shape)",
         "value": ws * nsub / (ms_per_step / 1e3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -349,6 +357,7 @@ def run_tracking_step(args, ws, rank, local):
                    "nsub": nsub, "members": nmem, "snapshot_particles": nsnap,
                    "l2": "flushed before each timed step (256 MB write)"},
         "phase_ms_per_step": {"table_fill": fill_ms, "resolve_gather": rg_ms, "unbind": un_ms,
+                              "properties": pr_ms,
                               "tree": st["tree_ms"] / args.steps,
                               "walk": st["walk_ms"] / args.steps},
         "roofline": {"kernel": "ID re-resolve + gather phase", "bound": "hbm",

@@ -80,6 +80,11 @@ class hbtu_props(C.Structure):
     ]
 
 
+class hbtu_core(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("sigma_r", C.c_float), ("vel", C.c_float * 3),
+                ("sigma_v", C.c_float)]
+
+
 class hbtu_stats(C.Structure):
     _fields_ = [
         ("total_ms", C.c_double), ("tree_ms", C.c_double), ("walk_ms", C.c_double),
@@ -120,6 +125,9 @@ SIGNATURES = {
     "hbtu_subhalo_properties": (C.c_int, [C.c_void_p, C.POINTER(hbtu_particles), C.c_int64,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_int32, C.c_void_p]),
+    "hbtu_merge_detect": (C.c_int, [C.c_void_p, C.POINTER(hbtu_particles), C.c_int64,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "hbtu_index_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "hbtu_index_destroy": (C.c_int, [C.c_void_p]),
     "hbtu_index_fill": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,

@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "device_common.cuh"
@@ -349,6 +350,7 @@ extern "C" hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_partic
   cudaStream_t st = h->stream;
   const bool host = p->location == HBTU_HOST;
   char *mem = nullptr;
+  const long long launches0 = g_launches;
   try {
     // results on the host for the plan
     std::vector<hbtu_result> hres;
@@ -397,12 +399,26 @@ extern "C" hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_partic
         2 * a256(8 * (nT + 1)) + 3 * a256(4 * nT) + 2 * a256(8 * nsub) + a256(8 * nsub) +
         a256(8 * 12 * nC) + a256(4 * nC) + 2 * a256(4 * nsub) + a256(sizeof(hbtu_props) * nsub) +
         a256(scan_tmp_bytes(T + 1)) + 256;
-    if (cudaMalloc(&mem, total) != cudaSuccess) {
-      cudaGetLastError();
-      mem = nullptr;
-      h->err = "subhalo properties: device buffers";
-      return HBTU_ERR_OUT_OF_MEMORY;
+    // the handle's workspace (the unbinding's buffers are larger, so it is
+    // normally in place already)
+    if (total > h->ws_bytes) {
+      if (h->ws) {
+        cudaStreamSynchronize(st);
+        cudaFree(h->ws);
+        h->ws = nullptr;
+        h->ws_bytes = 0;
+      }
+      const size_t bytes = total + total / 4;
+      if (cudaMalloc(&h->ws, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        h->ws = nullptr;
+        h->err = "subhalo properties: device workspace of " + std::to_string(bytes) +
+                 " bytes could not be allocated";
+        return HBTU_ERR_OUT_OF_MEMORY;
+      }
+      h->ws_bytes = bytes;
     }
+    mem = h->ws;
     size_t o = 0;
     auto take = [&](size_t bytes) {
       char *q = mem + o;
@@ -503,8 +519,7 @@ extern "C" hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_partic
     HBTU_CUDA(cudaMemcpyAsync(hso.data(), d_so, 8 * nsub, cudaMemcpyDeviceToHost, st));
     HBTU_CUDA(cudaMemcpyAsync(hflags, d_flags, sizeof(hflags), cudaMemcpyDeviceToHost, st));
     HBTU_CUDA(cudaStreamSynchronize(st));
-    cudaFree(mem);
-    mem = nullptr;
+    h->stats.kernel_launches += g_launches - launches0;
     if (hflags[F_SORT]) {
       h->err = "subhalo properties: radix sort look-back wait ran out";
       return HBTU_ERR_CUDA;
@@ -519,7 +534,6 @@ extern "C" hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_partic
         out[s].r200crit_comoving = (float)std::pow((double)(out[s].m200crit / rho_vir), 1.0 / 3);
     return HBTU_OK;
   } catch (const CudaError &e) {
-    if (mem) cudaFree(mem);
     h->err = e.what;
     return HBTU_ERR_CUDA;
   }

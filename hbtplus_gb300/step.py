@@ -5,12 +5,15 @@ turns them back into the new snapshot's particles through the snapshot's
 ID table (ParticleSnapshot_t::GetIndices, src/snapshot.h:191-224,
 src/hash_remote.tpp; ParticleExchanger_t::QueryParticles,
 src/particle_exchanger.h:194-208), then unbinds every subhalo
-(SubhaloSnapshot_t::RefineParticles, src/subhalo_unbind.cpp:460-516).  Here the
-whole step stays on the GPU:
+(SubhaloSnapshot_t::RefineParticles, src/subhalo_unbind.cpp:460-516), and
+computes each subhalo's profile and shape (Subhalo_t::CalculateProfileProperties
+and ::CalculateShape, called at the end of SubhaloSnapshot_t::UpdateTracks,
+src/subhalo_tracking.cpp:901-906).  Here the whole step stays on the GPU:
 
     step = TrackingStep(unbinder, flat=False)
     step.load_snapshot(ids, pos, vel, mass, type)        # CUDA tensors; fills the table
-    out = step.run(offsets, member_ids, states)          # re-resolve, gather, unbind
+    out, index = step.run(offsets, member_ids, states,   # re-resolve, gather, unbind,
+                          properties=dict(snapshot_index=7))   # profile and shape
 """
 from __future__ import annotations
 
@@ -56,9 +59,12 @@ class TrackingStep:
             raise ValueError("a member ID is not in the snapshot")
         return {k: v.index_select(0, index) for k, v in self.snap.items()}
 
-    def run(self, offsets, member_ids, states):
+    def run(self, offsets, member_ids, states, properties=None):
         """Re-resolve, gather and unbind every subhalo; returns (order, energy,
-        results bytes) as CUDA tensors and the resolved positions."""
+        results bytes) as CUDA tensors and the resolved positions.  With
+        ``properties`` (a dict of snapshot_index and, optionally, the
+        last_max_vmax and last_snap arrays of the subhaloes), out["props"]
+        also holds every subhalo's profile and shape (hbtu_props array)."""
         index = self.resolve(member_ids)
         batch = self.gather(index)
         n = member_ids.numel()
@@ -69,4 +75,10 @@ class TrackingStep:
                    res=torch.empty(nsub * C.sizeof(_lib.hbtu_result), dtype=torch.uint8,
                                    device=dev))
         self.ub.unbind_batch_device(batch, offsets, states, out)
+        if properties is not None:
+            out["props"] = self.ub.subhalo_properties_device(
+                batch, offsets, out["order"], out["res"],
+                last_max_vmax=properties.get("last_max_vmax"),
+                last_snap=properties.get("last_snap"),
+                snapshot_index=int(properties.get("snapshot_index", 0)))
         return out, index

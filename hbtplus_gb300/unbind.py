@@ -368,6 +368,36 @@ class Unbinder:
         del keep
         return [props_to_dict(out[s]) for s in range(nsub)]
 
+    def merge_detect(self, parts: dict, list_off, nbound, host, mostbound_pos, mostbound_vel,
+                     snapshot_index: int, sink):
+        """Cores and trap detection of the merging step (hbtu_merge_detect):
+        ``parts`` holds pos, vel and mass of every subhalo's list (bound
+        first), concatenated by ``list_off``.  Returns (sink, sink_snap,
+        merged, cores); sink_snap is -1 where nothing was trapped now."""
+        off = np.ascontiguousarray(list_off, np.int64)
+        nsub = len(off) - 1
+        n = int(off[-1])
+        d = dict(parts)
+        d.setdefault("id", np.zeros(n, np.int64))
+        p, keep = self._host_particles(d)
+        nb = np.ascontiguousarray(nbound, np.int64)
+        hs = np.ascontiguousarray(host, np.int64)
+        mbp = np.ascontiguousarray(mostbound_pos, np.float32)
+        mbv = np.ascontiguousarray(mostbound_vel, np.float32)
+        sk = np.ascontiguousarray(sink, np.int64).copy()
+        snap = np.full(max(nsub, 1), -1, np.int32)
+        merged = np.zeros(max(nsub, 1), np.int32)
+        cores = (_lib.hbtu_core * max(nsub, 1))()
+        rc = self.lib.hbtu_merge_detect(self.handle, C.byref(p), nsub, _ptr(off), _ptr(nb),
+                                        _ptr(hs), _ptr(mbp), _ptr(mbv), int(snapshot_index),
+                                        _ptr(sk), _ptr(snap), _ptr(merged), C.addressof(cores))
+        _lib.check(rc, self.handle)
+        del keep
+        cd = [dict(pos=np.array(list(cores[s].pos), np.float32), sigma_r=cores[s].sigma_r,
+                   vel=np.array(list(cores[s].vel), np.float32), sigma_v=cores[s].sigma_v)
+              for s in range(nsub)]
+        return sk[:nsub], snap[:nsub], merged[:nsub], cd
+
     def subhalo_properties_device(self, dev: dict, offsets: np.ndarray, order, res,
                                   last_max_vmax=None, last_snap=None, snapshot_index: int = 0):
         """subhalo_properties on device-resident torch tensors: ``dev`` holds

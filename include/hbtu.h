@@ -274,6 +274,39 @@ hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_particles *p, int
                                     const int32_t *last_snap, int32_t snapshot_index,
                                     hbtu_props *out);
 
+/* Core of a subhalo as the merging step sees it (SubHelper_t,
+ * src/subhalo_merge.cpp:14-26): mean position and velocity of its first
+ * min(Nbound, 20) particles (NumPartCoreMax) and their dispersions. */
+typedef struct hbtu_core {
+  float pos[3];   /* ComovingPosition */
+  float sigma_r;  /* ComovingSigmaR */
+  float vel[3];   /* PhysicalVelocity */
+  float sigma_v;  /* PhysicalSigmaV */
+} hbtu_core;
+
+/* FillCores + DetectTraps, the first half of SubhaloSnapshot_t::MergeSubhalos
+ * (src/subhalo_merge.cpp:30-180, :187-199), for every subhalo at once.
+ *   p: the particles of every subhalo's list, concatenated, bound first
+ *      (list_off: nsub+1 offsets, host memory); pos, vel and mass are read;
+ *   nbound[s]: Nbound; host[s]: HostTrackId as local index (-1: none; the
+ *      other top-level subhaloes of a halo count as nested in its central,
+ *      GlueHeadNests); mostbound_pos/vel[3*s]: ComovingMostBoundPosition,
+ *      PhysicalMostBoundVelocity;
+ *   sink[s]: SinkTrackId on entry (-1: not trapped; such a subhalo is skipped)
+ *      and on return; a subhalo trapped now gets sink_snap[s] = snapshot_index
+ *      (other entries are left as given); merged[s] = 1 marks a subhalo that
+ *      swallows a subhalo with Nbound > 1 (Helpers[].IsMerged), else 0;
+ *   cores (may be NULL): every subhalo's core.
+ * All arrays but p's are host memory.  The merge itself (MergeTo: the union
+ * of particle lists by Id) and the re-unbinding of merged subhaloes
+ * (hbtu_unbind_batch) follow on the caller's side.  A host chain with a
+ * cycle returns HBTU_ERR_INVALID_ARGUMENT. */
+hbtu_status hbtu_merge_detect(hbtu_handle *h, const hbtu_particles *p, int64_t nsub,
+                              const int64_t *list_off, const int64_t *nbound, const int64_t *host,
+                              const float *mostbound_pos, const float *mostbound_vel,
+                              int32_t snapshot_index, int64_t *sink, int32_t *sink_snap,
+                              int32_t *merged, hbtu_core *cores);
+
 /* Particle-ID -> index tables, the ID re-resolve of the unbinding step's
  * callers (IndexTable_t, src/hash.h:47-112; filled from a snapshot's IDs by
  * ParticleSnapshot_t, src/snapshot.h:191-224, and queried by GetIndex /

@@ -1028,3 +1028,119 @@ int hbto_subhalo_properties(const hbto_params *par, int64_t nbound, const float 
   }
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Merging: SubHelper_t::BuildPosition / BuildVelocity, SinkDistance and
+ * DetectTraps (src/subhalo_merge.cpp:30-165).                               */
+#define CORE_PARTICLES 20 /* NumPartCoreMax, subhalo_merge.cpp:11 */
+#define DELTA_CRIT 2.f    /* DeltaCrit, :12 */
+
+static void build_core(const dpar *d, int64_t nb, const float *pos, const float *vel,
+                       const float *mass, hbto_core *c)
+{
+  memset(c, 0, sizeof(*c));
+  if (nb <= 0) return; /* :32-36, :83-87 (position left unset there) */
+  if (nb == 1) {       /* :37-42, :88-93 */
+    for (int j = 0; j < 3; j++) {
+      c->pos[j] = pos[j];
+      c->vel[j] = vel[j];
+    }
+    return;
+  }
+  const int64_t np = nb > CORE_PARTICLES ? CORE_PARTICLES : nb;
+  double sx[3] = {0, 0, 0}, sx2[3] = {0, 0, 0}, origin[3] = {0, 0, 0}, msum = 0.;
+  if (d->periodic)
+    for (int j = 0; j < 3; j++) origin[j] = pos[j];
+  for (int64_t i = 0; i < np; i++) { /* :55-70 */
+    const float m = mass[i];
+    msum += m;
+    for (int j = 0; j < 3; j++) {
+      double dx;
+      if (d->periodic)
+        dx = nearest_d((double)pos[3 * i + j] - origin[j], d);
+      else
+        dx = pos[3 * i + j];
+      sx[j] += dx * m;
+      sx2[j] += dx * dx * m;
+    }
+  }
+  for (int j = 0; j < 3; j++) { /* :72-80 */
+    sx[j] /= msum;
+    sx2[j] /= msum;
+    c->pos[j] = (float)sx[j];
+    if (d->periodic) c->pos[j] = (float)((double)c->pos[j] + origin[j]);
+    sx2[j] -= sx[j] * sx[j];
+  }
+  c->sigma_r = (float)sqrt(sx2[0] + sx2[1] + sx2[2]);
+  double sv[3] = {0, 0, 0}, sv2[3] = {0, 0, 0};
+  msum = 0.;
+  for (int64_t i = 0; i < np; i++) { /* :104-116 */
+    const float m = mass[i];
+    msum += m;
+    for (int j = 0; j < 3; j++) {
+      const double dv = vel[3 * i + j];
+      sv[j] += dv * m;
+      sv2[j] += dv * dv * m;
+    }
+  }
+  for (int j = 0; j < 3; j++) { /* :118-124 */
+    sv[j] /= msum;
+    sv2[j] /= msum;
+    c->vel[j] = (float)sv[j];
+    sv2[j] -= sv[j] * sv[j];
+  }
+  c->sigma_v = (float)sqrt(sv2[0] + sv2[1] + sv2[2]);
+}
+
+/* SinkDistance (:128-133) with PeriodicDistance (config_parser.h:143-156)
+ * and Distance (mymath.h:184-187), in float. */
+static float sink_distance(const dpar *d, const float *mbp, const float *mbv, const hbto_core *c)
+{
+  float dx[3], dv[3];
+  for (int j = 0; j < 3; j++) {
+    dx[j] = c->pos[j] - mbp[j];
+    if (d->periodic) dx[j] = nearest_f(dx[j], d);
+    dv[j] = c->vel[j] - mbv[j];
+  }
+  const float r = sqrtf(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+  const float v = sqrtf(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+  return r / c->sigma_r + v / c->sigma_v;
+}
+
+int hbto_merge_detect(const hbto_params *par, int64_t nsub, const int64_t *list_off,
+                      const float *pos, const float *vel, const float *mass,
+                      const int64_t *nbound, const int64_t *host, const float *mb_pos,
+                      const float *mb_vel, int32_t isnap, int64_t *sink, int32_t *sink_snap,
+                      int32_t *merged, hbto_core *cores)
+{
+  dpar d;
+  derive(par, &d);
+  hbto_core *c = malloc((size_t)(nsub > 0 ? nsub : 1) * sizeof(hbto_core));
+  for (int64_t s = 0; s < nsub; s++) { /* FillCores, :172-180 */
+    const int64_t o = list_off[s];
+    int64_t nb = nbound[s];
+    if (nb > list_off[s + 1] - o) nb = list_off[s + 1] - o;
+    build_core(&d, nb, pos + 3 * o, vel + 3 * o, mass + o, c + s);
+  }
+  int rc = 0;
+  for (int64_t s = 0; s < nsub; s++) { /* DetectTraps, :135-160 */
+    if (sink[s] >= 0) continue;       /* IsTrapped */
+    int64_t h = host[s], steps = 0;
+    while (h >= 0) {
+      if (++steps > nsub) {
+        rc = -1;
+        break;
+      }
+      if (nbound[h] > 1 && sink_distance(&d, mb_pos + 3 * s, mb_vel + 3 * s, c + h) < DELTA_CRIT) {
+        sink[s] = h;
+        sink_snap[s] = isnap;
+        if (nbound[s] > 1) merged[h] = 1;
+        break;
+      }
+      h = host[h];
+    }
+  }
+  if (cores) memcpy(cores, c, (size_t)nsub * sizeof(hbto_core));
+  free(c);
+  return rc;
+}

@@ -138,6 +138,31 @@ int hbto_subhalo_properties(const hbto_params *par, int64_t nbound, const float 
                             float last_max_vmax, int32_t last_snap, int32_t snapshot_index,
                             hbto_props *out);
 
+/* Core of a subhalo as the merging step sees it (SubHelper_t,
+ * src/subhalo_merge.cpp:14-26): mean position and velocity of its first
+ * min(Nbound, 20) particles and their dispersions. */
+typedef struct {
+  float pos[3];
+  float sigma_r;
+  float vel[3];
+  float sigma_v;
+} hbto_core;
+
+/* FillCores and DetectTraps of SubhaloSnapshot_t::MergeSubhalos
+ * (src/subhalo_merge.cpp:30-180): subhalo s holds particles
+ * [list_off[s], list_off[s+1]) of pos/vel/mass, bound first; host[s] its
+ * HostTrackId (-1: none); mb_pos/mb_vel its ComovingMostBoundPosition and
+ * PhysicalMostBoundVelocity.  sink[s] is SinkTrackId on entry (-1: not yet
+ * trapped) and on exit; a subhalo trapped now gets sink_snap[s] = isnap (other
+ * entries are left alone), and its host merged[host] = 1 when the subhalo has
+ * Nbound > 1.  cores may be NULL.  Returns -1 if a host chain is longer than
+ * nsub (a cycle). */
+int hbto_merge_detect(const hbto_params *par, int64_t nsub, const int64_t *list_off,
+                      const float *pos, const float *vel, const float *mass,
+                      const int64_t *nbound, const int64_t *host, const float *mb_pos,
+                      const float *mb_vel, int32_t isnap, int64_t *sink, int32_t *sink_snap,
+                      int32_t *merged, hbto_core *cores);
+
 /* Particle-ID -> index tables (src/hash.h:47-112, src/hash.tpp, src/hash_remote.tpp).
  * Fill a table with the pairs (keys[i], values[i]), i < n (KeyList_t::GetKey and
  * ::GetIndex), then look up every query: out[j] = GetIndex(queries[j]), or

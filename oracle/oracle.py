@@ -69,6 +69,11 @@ class Result(C.Structure):
     ]
 
 
+class Core(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("sigma_r", C.c_float), ("vel", C.c_float * 3),
+                ("sigma_v", C.c_float)]
+
+
 class Props(C.Structure):
     _fields_ = [
         ("rmax_comoving", C.c_float), ("vmax_physical", C.c_float),
@@ -269,6 +274,90 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"ref_recursive_unbind failed ({rc})")
         return out_off, out_pos[:out_off[-1]], [result_dict(res[s]) for s in range(nsub)]
+
+    def merge_detect(self, params: dict, list_off, pos, vel, mass, nbound, host, mb_pos, mb_vel,
+                     isnap: int, sink):
+        """FillCores + DetectTraps (C restatement): returns (sink, sink_snap,
+        merged, cores) with sink_snap -1 where nothing was trapped now."""
+        lo = np.ascontiguousarray(list_off, np.int64)
+        nsub = len(lo) - 1
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1)
+        vel = np.ascontiguousarray(vel, np.float32).reshape(-1)
+        mass = np.ascontiguousarray(mass, np.float32)
+        nb = np.ascontiguousarray(nbound, np.int64)
+        host = np.ascontiguousarray(host, np.int64)
+        mbp = np.ascontiguousarray(mb_pos, np.float32).reshape(-1)
+        mbv = np.ascontiguousarray(mb_vel, np.float32).reshape(-1)
+        sink = np.ascontiguousarray(sink, np.int64).copy()
+        snap = np.full(max(nsub, 1), -1, np.int32)
+        merged = np.zeros(max(nsub, 1), np.int32)
+        cores = (Core * max(nsub, 1))()
+        fn = self.lib.hbto_merge_detect
+        fn.restype = C.c_int
+        rc = fn(C.byref(make_params(params)), C.c_int64(nsub), _p(lo, C.c_int64),
+                _p(pos, C.c_float), _p(vel, C.c_float), _p(mass, C.c_float), _p(nb, C.c_int64),
+                _p(host, C.c_int64), _p(mbp, C.c_float), _p(mbv, C.c_float), C.c_int32(isnap),
+                _p(sink, C.c_int64), _p(snap, C.c_int32), _p(merged, C.c_int32), cores)
+        if rc != 0:
+            raise RuntimeError("hbto_merge_detect: a host chain has a cycle")
+        cd = [dict(pos=np.array(list(cores[s].pos), np.float32), sigma_r=cores[s].sigma_r,
+                   vel=np.array(list(cores[s].vel), np.float32), sigma_v=cores[s].sigma_v)
+              for s in range(nsub)]
+        return sink[:nsub], snap[:nsub], merged[:nsub], cd
+
+    def merge_subhalos(self, params: dict, state: dict, isnap: int, relax: float = 3.0):
+        """The reference's SubhaloSnapshot_t::MergeSubhalos (reference build
+        only).  state: every subhalo's list (id, pos, vel, mass, type rows,
+        list_off, bound first), nbound, frames, nest_off/nest_idx,
+        group_off/group_idx (central first), heads_off/heads_idx, sink, death.
+        Returns dict(off, id, energy, sink, death, sink_snap, results)."""
+        if not self.reference:
+            raise ValueError("exists in the reference build only")
+        a = {k: np.ascontiguousarray(state[k], np.int64)
+             for k in ("list_off", "nbound", "nest_off", "nest_idx", "group_off", "group_idx",
+                       "heads_off", "heads_idx", "sink", "id")}
+        death = np.ascontiguousarray(state["death"], np.int32)
+        pos = np.ascontiguousarray(state["pos"], np.float32).reshape(-1)
+        vel = np.ascontiguousarray(state["vel"], np.float32).reshape(-1)
+        mass = np.ascontiguousarray(state["mass"], np.float32)
+        typ = np.ascontiguousarray(state["type"], np.int32)
+        nsub = len(a["list_off"]) - 1
+        nhalo = len(a["group_off"]) - 1
+        sts = (State * max(nsub, 1))()
+        for s in range(nsub):
+            for j in range(3):
+                sts[s].ref_pos[j] = float(state["ref_pos"][s][j])
+                sts[s].ref_vel[j] = float(state["ref_vel"][s][j])
+                sts[s].mostbound_pos[j] = float(state["mostbound_pos"][s][j])
+                sts[s].mostbound_vel[j] = float(state["mostbound_vel"][s][j])
+            lo = int(a["list_off"][s])
+            sts[s].mostbound_id = int(a["id"][lo]) if a["list_off"][s + 1] > lo else -1
+        cap = max(2 * int(a["list_off"][-1]), 1)
+        out_off = np.zeros(nsub + 1, np.int64)
+        out_id = np.zeros(cap, np.int64)
+        out_e = np.zeros(cap, np.float32)
+        sink = np.zeros(max(nsub, 1), np.int64)
+        dout = np.zeros(max(nsub, 1), np.int32)
+        ssnap = np.zeros(max(nsub, 1), np.int32)
+        res = (Result * max(nsub, 1))()
+        fn = self.lib.ref_merge_subhalos
+        fn.restype = C.c_int
+        rc = fn(C.byref(make_params(params)), C.c_double(relax), C.c_int32(isnap),
+                C.c_int64(nsub), _p(a["list_off"], C.c_int64), _p(a["id"], C.c_int64),
+                _p(pos, C.c_float), _p(vel, C.c_float), _p(mass, C.c_float), _p(typ, C.c_int32),
+                _p(a["nbound"], C.c_int64), sts, _p(a["nest_off"], C.c_int64),
+                _p(a["nest_idx"], C.c_int64), C.c_int64(nhalo), _p(a["group_off"], C.c_int64),
+                _p(a["group_idx"], C.c_int64), _p(a["heads_off"], C.c_int64),
+                _p(a["heads_idx"], C.c_int64), _p(a["sink"], C.c_int64), _p(death, C.c_int32),
+                C.c_int64(cap), _p(out_off, C.c_int64), _p(out_id, C.c_int64),
+                _p(out_e, C.c_float), _p(sink, C.c_int64), _p(dout, C.c_int32),
+                _p(ssnap, C.c_int32), res)
+        if rc != 0:
+            raise RuntimeError(f"ref_merge_subhalos failed ({rc})")
+        n = int(out_off[-1])
+        return dict(off=out_off, id=out_id[:n], energy=out_e[:n], sink=sink[:nsub],
+                    death=dout[:nsub], sink_snap=ssnap[:nsub],
+                    results=[result_dict(res[s]) for s in range(nsub)])
 
     def partition(self, E: np.ndarray):
         E = np.ascontiguousarray(E, np.float32).copy()

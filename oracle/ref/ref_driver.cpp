@@ -184,7 +184,61 @@ struct IdOnly_t {
   HBTInt Id;
 };
 
+/* A SubhaloSnapshot_t holding only what MergeSubhalos reads: the subhaloes,
+ * the halo membership table, the snapshot index and the cosmology. */
+class MergeSnap_t : public SubhaloSnapshot_t
+{
+public:
+  MergeSnap_t(const hbto_params *p, int isnap)
+  {
+    Cosmology.ScaleFactor = p->scale_factor;
+    Cosmology.Hz = p->hubble;
+    Cosmology.OmegaM0 = 0.3;
+    Cosmology.OmegaLambda0 = 0.7;
+    Cosmology.OmegaZ = 0.3;
+    SnapshotIndex = isnap;
+    SnapshotId = isnap;
+  }
+};
+
 }  // namespace
+
+/* Stand-ins for the SubhaloSnapshot_t members whose own definitions sit in
+ * files this harness does not compile (they need MPI and HDF5).  The HDF5
+ * type set-up is never used here.  GlueHeadNests / UnglueHeadNests restate
+ * src/subhalo_tracking.cpp:843-874: while merging, the other top-level
+ * subhaloes of a halo join its central's nest, and leave it afterwards. */
+void SubhaloSnapshot_t::BuildHDFDataType() {}
+herr_t H5Tclose(hid_t) { return 0; }
+void SubhaloSnapshot_t::GlueHeadNests()
+{
+#pragma omp single
+  {
+    RootNestSize.resize(MemberTable.SubGroups.size());
+    for (HBTInt h = 0; h < (HBTInt)RootNestSize.size(); h++) {
+      auto &group = MemberTable.SubGroups[h];
+      if (group.size() == 0) {
+        RootNestSize[h] = 0;
+        continue;
+      }
+      auto &nest = Subhalos[group[0]].NestedSubhalos;
+      RootNestSize[h] = nest.size();
+      auto &heads = MemberTable.SubGroupsOfHeads[h];
+      nest.insert(nest.end(), heads.begin() + 1, heads.end());
+    }
+  }
+}
+void SubhaloSnapshot_t::UnglueHeadNests()
+{
+#pragma omp single
+  {
+    for (HBTInt h = 0; h < (HBTInt)RootNestSize.size(); h++) {
+      auto &group = MemberTable.SubGroups[h];
+      if (group.size()) Subhalos[group[0]].NestedSubhalos.resize(RootNestSize[h]);
+    }
+    RootNestSize.clear();
+  }
+}
 
 extern "C" {
 
@@ -395,5 +449,77 @@ int ref_binding_energies(const hbto_params *par, int64_t n, const float *pos, co
 }
 
 void ref_srand48(long seed) { srand48(seed); }
+
+/* SubhaloSnapshot_t::MergeSubhalos (src/subhalo_merge.cpp:187-220) with
+ * MergeTrappedSubhalos on, at snapshot isnap, over subhaloes after their
+ * unbinding: subhalo s holds the particles [list_off[s], list_off[s+1]) of
+ * the arrays (bound first), Nbound nbound[s], frames st[s]
+ * (ref_pos/ref_vel = ComovingAveragePosition/PhysicalAverageVelocity), nested
+ * subhaloes nest_idx[nest_off[s]..), SinkTrackId sink_in[s] and
+ * SnapshotIndexOfDeath death_in[s]; halo h has members
+ * group_idx[group_off[h]..) (central first) and top-level subhaloes
+ * heads_idx[heads_off[h]..) (central first).  Output per subhalo: the
+ * particle Ids of its list (out_off, out_id), their energies where the
+ * re-unbinding kept them (out_energy), SinkTrackId, SnapshotIndexOfDeath,
+ * SnapshotIndexOfSink, and its results. */
+int ref_merge_subhalos(const hbto_params *par, double relax_factor, int32_t isnap, int64_t nsub,
+                       const int64_t *list_off, const int64_t *id, const float *pos,
+                       const float *vel, const float *mass, const int32_t *type,
+                       const int64_t *nbound, const hbto_state *st, const int64_t *nest_off,
+                       const int64_t *nest_idx, int64_t nhalo, const int64_t *group_off,
+                       const int64_t *group_idx, const int64_t *heads_off,
+                       const int64_t *heads_idx, const int64_t *sink_in, const int32_t *death_in,
+                       int64_t out_capacity, int64_t *out_off, int64_t *out_id,
+                       float *out_energy, int64_t *sink_out, int32_t *death_out,
+                       int32_t *sink_snap_out, hbto_result *res)
+{
+  setup(par);
+  HBTConfig.SourceSubRelaxFactor = relax_factor;
+  HBTConfig.MergeTrappedSubhalos = true;
+  omp_set_num_threads(1);
+  omp_set_max_active_levels(1);
+  std::vector<HBTInt> members(group_idx, group_idx + group_off[nhalo]);
+  std::vector<MemberShipTable_t::MemberList_t> views(nhalo);
+  for (int64_t h = 0; h < nhalo; h++)
+    views[h].Bind(group_off[h + 1] - group_off[h], members.data() + group_off[h]);
+  MergeSnap_t snap(par, isnap);
+  snap.Subhalos.resize(nsub);
+  for (int64_t s = 0; s < nsub; s++) {
+    Subhalo_t &sub = snap.Subhalos[s];
+    const int64_t o = list_off[s], n = list_off[s + 1] - o;
+    fill_subhalo(sub, n, id + o, pos + 3 * o, vel + 3 * o, mass + o, type ? type + o : nullptr,
+                 st + s);
+    sub.Nbound = nbound[s];
+    sub.NestedSubhalos.assign(nest_idx + nest_off[s], nest_idx + nest_off[s + 1]);
+    sub.SinkTrackId = sink_in[s];
+    sub.SnapshotIndexOfDeath = death_in[s];
+    sub.CountParticles();
+  }
+  snap.MemberTable.SubGroups.Bind(nhalo, views.data());
+  snap.MemberTable.SubGroupsOfHeads.resize(nhalo);
+  for (int64_t h = 0; h < nhalo; h++)
+    snap.MemberTable.SubGroupsOfHeads[h].assign(heads_idx + heads_off[h],
+                                                heads_idx + heads_off[h + 1]);
+  srand(0);
+  snap.MergeSubhalos();
+  const int64_t ntot = list_off[nsub];
+  std::vector<int64_t> ids, ipos;
+  sorted_ids(ntot, id, ids, ipos);
+  out_off[0] = 0;
+  for (int64_t s = 0; s < nsub; s++) {
+    const Subhalo_t &sub = snap.Subhalos[s];
+    const int64_t n = sub.Particles.size();
+    if (out_off[s] + n > out_capacity) return -1;
+    std::vector<int64_t> order(n);
+    read_subhalo(sub, n, ipos.data(), ids.data(), order.data(), out_energy + out_off[s], res + s,
+                 ntot);
+    for (int64_t i = 0; i < n; i++) out_id[out_off[s] + i] = sub.Particles[i].Id;
+    sink_out[s] = sub.SinkTrackId;
+    death_out[s] = sub.SnapshotIndexOfDeath;
+    sink_snap_out[s] = sub.SnapshotIndexOfSink;
+    out_off[s + 1] = out_off[s] + n;
+  }
+  return 0;
+}
 
 }  // extern "C"

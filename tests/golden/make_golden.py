@@ -205,6 +205,113 @@ def forest_cases(ref):
           f"nbound {[int(r['nbound']) for r in res]}")
 
 
+def merge_case(seed=140, n_scale=1.0):
+    """Subhaloes for MergeSubhalos, each with its own particles: in halo A a
+    central, a satellite sitting in its core (it sinks), a satellite passing
+    fast (it does not), a sub-satellite in that satellite's core (it sinks into
+    its host), a satellite of the sinking one, an orphan at the central's
+    centre and a satellite trapped at an earlier snapshot but still alive; in
+    halo B a central and a second top-level subhalo in its core (glued to the
+    central's nest while merging); a field subhalo.  The central of A lists
+    the sinking satellite's outer particles too (a tail it received while
+    unbinding), so the merge has duplicate IDs to drop."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    box = 100.0
+    specs = [  # (n, r200, parent, offset from parent centre, bulk speed, halo)
+        (3000, 0.22, None, 0.0, 0.0, 0),     # 0: central of halo A
+        (600, 0.08, 0, 0.0005, 1.0, 0),      # 1: sits in 0's core: sinks into 0
+        (500, 0.07, 0, 0.15, 400.0, 0),      # 2: passes fast: stays
+        (200, 0.04, 2, 0.0003, 1.0, 0),      # 3: in 2's core: sinks into 2
+        (150, 0.03, 1, 0.03, 80.0, 0),       # 4: satellite of 1
+        (1, 0.01, 0, 0.0005, 0.0, 0),        # 5: orphan at 0's centre
+        (120, 0.03, 0, 0.05, 100.0, 0),      # 6: trapped before (SinkTrackId 0), alive
+        (2000, 0.18, None, 0.0, 0.0, 1),     # 7: central of halo B
+        (700, 0.08, None, 0.0005, 1.0, 1),   # 8: second head of B, in 7's core
+        (400, 0.06, None, 0.0, 0.0, 2),      # 9: field subhalo
+    ]
+    centres, subs = [], []
+    for k, (n, r200, parent, off, bulk, halo) in enumerate(specs):
+        n = max(1, int(n * n_scale)) if n > 1 else 1
+        anchor = parent if parent is not None else (7 if k == 8 else None)
+        if anchor is None:
+            c = rng.uniform(10.0, 90.0, size=3)
+            v = np.zeros(3)
+        else:
+            u = rng.normal(size=3)
+            c = centres[anchor][0] + off * u / np.linalg.norm(u)
+            w = rng.normal(size=3)
+            v = centres[anchor][1] + bulk * w / np.linalg.norm(w)
+        centres.append((c, v))
+        subs.append(S.nfw_subhalo(rng, n, r200, 8.0, contaminant_frac=0.1 if n > 1 else 0.0,
+                                  center=c, bulk_velocity=v, box=box))
+    S._assign_ids(rng, subs)
+    # central 0 also holds satellite 1's last 60 particles
+    tail = {k: subs[1][k][-max(1, int(60 * n_scale)):] for k in ("id", "pos", "vel", "mass",
+                                                                    "type")}
+    for k in tail:
+        subs[0][k] = np.concatenate([subs[0][k], tail[k]])
+    nests = [[] for _ in specs]
+    for k, sp in enumerate(specs):
+        if sp[2] is not None:
+            nests[sp[2]].append(k)
+    groups = [[0, 1, 2, 3, 4, 5, 6], [7, 8], [9]]
+    heads = [[0], [7, 8], [9]]
+    sink = np.full(len(specs), -1, np.int64)
+    sink[6] = 0
+    return subs, nests, groups, heads, sink
+
+
+def merge_state(unbind, params, case):
+    """The subhaloes after their unbinding (bound particles first), the input
+    of MergeSubhalos: unbind(params, sub) -> (order, result)."""
+    subs, nests, groups, heads, sink = case
+    rows, nbound, frames = [], [], {k: [] for k in ("ref_pos", "ref_vel", "mostbound_pos",
+                                                     "mostbound_vel")}
+    for sub in subs:
+        order, r = unbind(params, sub)
+        rows.append({k: np.asarray(sub[k])[order] for k in ("id", "pos", "vel", "mass", "type")})
+        nbound.append(int(r["nbound"]))
+        for k in frames:
+            frames[k].append(np.asarray(r[k], np.float32))
+    def flat(lists):
+        off = np.concatenate([[0], np.cumsum([len(x) for x in lists])]).astype(np.int64)
+        idx = np.array([c for x in lists for c in x], np.int64)
+        return off, idx
+    st = {k: np.concatenate([r[k] for r in rows]) for k in ("id", "pos", "vel", "mass", "type")}
+    st["list_off"] = np.concatenate([[0], np.cumsum([len(r["id"]) for r in rows])]).astype(
+        np.int64)
+    st["nbound"] = np.array(nbound, np.int64)
+    st.update({k: np.array(v) for k, v in frames.items()})
+    st["nest_off"], st["nest_idx"] = flat(nests)
+    st["group_off"], st["group_idx"] = flat(groups)
+    st["heads_off"], st["heads_idx"] = flat(heads)
+    st["sink"] = np.asarray(sink, np.int64)
+    st["death"] = np.full(len(subs), -1, np.int32)
+    return st
+
+
+def merge_cases(ref):
+    p = S.default_params()
+
+    def unbind(params, sub):
+        o, _, r = ref.unbind(params, sub, nthreads=1)
+        return o, r
+
+    st = merge_state(unbind, p, merge_case())
+    out = ref.merge_subhalos(p, st, isnap=5, relax=3.0)
+    np.savez_compressed(
+        os.path.join(HERE, "merge_10.npz"),
+        **{f"in_{k}": v for k, v in st.items()},
+        **{f"par_{k}": np.asarray(v) for k, v in p.items()},
+        isnap=np.int32(5), relax=np.float64(3.0),
+        ref_off=out["off"], ref_id=out["id"], ref_energy=out["energy"], ref_sink=out["sink"],
+        ref_death=out["death"], ref_sink_snap=out["sink_snap"],
+        **{f"ref_{k}": np.array([r[k] for r in out["results"]]) for k in RESULT_KEYS})
+    print(f"merge_10: nbound {list(st['nbound'])} -> "
+          f"{[int(r['nbound']) for r in out['results']]}, sink {list(out['sink'])}, "
+          f"death {list(out['death'])}")
+
+
 PROPS_KEYS = ("rmax_comoving", "vmax_physical", "last_max_vmax_physical",
               "snapshot_of_last_max_vmax", "r2sigma_comoving", "rhalf_comoving",
               "r200crit_comoving", "m200crit", "inertial_tensor", "inertial_tensor_weighted")
@@ -278,8 +385,11 @@ if __name__ == "__main__":
         forest_cases(Oracle(reference=True))
     elif sys.argv[1:] == ["props"]:
         props_cases(Oracle(reference=True))
+    elif sys.argv[1:] == ["merge"]:
+        merge_cases(Oracle(reference=True))
     else:
         main()
         index_cases(Oracle(reference=True))
         forest_cases(Oracle(reference=True))
         props_cases(Oracle(reference=True))
+        merge_cases(Oracle(reference=True))

@@ -129,3 +129,33 @@ def recursive_unbind_oracle(orc, params, forest, relax=3.0):
         out.append(final[s][:ns])
         off.append(off[-1] + ns)
     return np.array(off, np.int64), np.concatenate(out), nbound
+
+
+class OracleUnbinder:
+    """The oracle behind the two calls hbtplus_gb300.merge makes of an
+    Unbinder (merge_detect, unbind_batch), so the host orchestration can be
+    checked on the CPU against the reference."""
+
+    def __init__(self, orc, params):
+        self.orc = orc
+        self.params = params
+
+    def merge_detect(self, parts, list_off, nbound, host, mb_pos, mb_vel, isnap, sink):
+        return self.orc.merge_detect(self.params, list_off, parts["pos"], parts["vel"],
+                                     parts["mass"], nbound, host, mb_pos, mb_vel, isnap, sink)
+
+    def unbind_batch(self, batch, check_status=True):
+        off = np.asarray(batch["offsets"], np.int64)
+        orders, energies, results = [], [], []
+        for s in range(len(off) - 1):
+            o0, o1 = int(off[s]), int(off[s + 1])
+            sub = {k: np.asarray(batch[k])[o0:o1] for k in ("id", "pos", "vel", "mass", "type")}
+            for k in ("ref_pos", "ref_vel", "mostbound_pos", "mostbound_vel"):
+                sub[k] = np.asarray(batch[k])[s]
+            sub["mostbound_id"] = int(batch["mostbound_id"][s])
+            o, e, r = self.orc.unbind(self.params, sub)
+            orders.append(o)
+            energies.append(e)
+            results.append(r)
+        cat = (lambda x, t: np.concatenate(x) if x else np.zeros(0, t))
+        return cat(orders, np.int64), cat(energies, np.float32), results

@@ -5,7 +5,7 @@ snapshot's ID table, the re-resolve of each subhalo's particle IDs
 Checks: the GPU re-resolve equals a host re-resolve (numpy), the gathered
 particles equal the host-gathered ones, and the unbinding of the gathered
 batch equals the same library's unbinding of the host-gathered batch bit for
-bit.  At full size (config 4: 20,000 subhaloes, 3e7 particles in a 200 Mpc/h
+bit, and so do the profile and shape of every subhalo.  At full size (config 4: 20,000 subhaloes, 3e7 particles in a 200 Mpc/h
 box, drift, 10% stripping) the same holds for 20 sampled subhaloes and every
 ID resolves."""
 import numpy as np
@@ -38,7 +38,8 @@ def run_step(d, flat=False):
                   mostbound_pos=d["mostbound_pos"], mostbound_vel=d["mostbound_vel"],
                   mostbound_id=d["mostbound_id"])
     states = ub.make_states(frames)
-    out, index = step.run(d["offsets"], T["member_id"], states)
+    out, index = step.run(d["offsets"], T["member_id"], states,
+                          properties=dict(snapshot_index=3))
     torch.cuda.synchronize()
     return ub, step, out, index.cpu().numpy(), states
 
@@ -70,6 +71,13 @@ def test_step_small_matches_host(flat):
     assert np.array_equal(out["order"].cpu().numpy(), order)
     assert np.array_equal(out["energy"].cpu().numpy(), energy, equal_nan=True)
     assert [r["nbound"] for r in gres] == [r["nbound"] for r in res]
+    # the step's profile and shape equal the host call on the host-gathered batch
+    from hbtplus_gb300.unbind import props_to_dict
+    hp = ub.subhalo_properties(b, order, res, snapshot_index=3)
+    for s in range(len(hp)):
+        g = props_to_dict(out["props"][s])
+        for k, v in hp[s].items():
+            assert np.array_equal(np.asarray(g[k]), np.asarray(v), equal_nan=True), (s, k)
     step.close()
     ub.close()
 
