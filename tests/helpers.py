@@ -9,7 +9,7 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 SINGLE_CASES = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
                       if not os.path.basename(f).startswith(("first_pass", "batch", "index", "forest",
-                                                                     "props")))
+                                                                     "props", "merge")))
 FIRST_PASS_CASES = sorted(os.path.basename(f)[:-4]
                           for f in glob.glob(os.path.join(GOLDEN, "first_pass_*.npz")))
 
