@@ -23,12 +23,17 @@ struct hbtu_index_table {
   hbtu_handle *h = nullptr;
   int flat = 0;
   int64_t n = 0, null_index = -1, kmin = 0, kmax = -1;
-  char *mem = nullptr;  // one allocation for everything below
+  // device memory is kept from fill to fill and only grows, so refilling a
+  // table every snapshot allocates nothing once it has reached its size
+  char *mem = nullptr;  // the table: everything below but aux
+  size_t cap = 0;
+  char *stage = nullptr;  // host-memory calls: staging of keys, values, queries
+  size_t stage_cap = 0;
+  unsigned long long *aux = nullptr;  // key min / max (biased), sort error flag
   int64_t *values = nullptr;
   unsigned long long *skeys = nullptr;  // mapped: sorted key - kmin
   int *spos = nullptr;                  // mapped: input position of each sorted key
   int *dense = nullptr;                 // flat: input position per key - kmin, -1 if none
-  unsigned long long *mm = nullptr;     // key min / max (biased)
 };
 
 namespace hbtu {
@@ -130,18 +135,47 @@ hbtu_status ix_fail(hbtu_index_table *t, hbtu_status st, const char *msg)
   return st;
 }
 
+// Forget the table's content (its memory stays for the next fill).
 void ix_release(hbtu_index_table *t)
 {
-  if (t->mem) cudaFree(t->mem);
-  t->mem = nullptr;
   t->values = nullptr;
   t->skeys = nullptr;
   t->spos = nullptr;
   t->dense = nullptr;
-  t->mm = nullptr;
   t->n = 0;
   t->kmin = 0;
   t->kmax = -1;
+}
+
+void ix_free(hbtu_index_table *t)
+{
+  ix_release(t);
+  if (t->mem) cudaFree(t->mem);
+  if (t->stage) cudaFree(t->stage);
+  if (t->aux) cudaFree(t->aux);
+  t->mem = t->stage = nullptr;
+  t->aux = nullptr;
+  t->cap = t->stage_cap = 0;
+}
+
+// Grow *buf to at least `bytes` (with headroom); false if that fails.
+bool ix_grow(hbtu_index_table *t, char **buf, size_t *cap, size_t bytes)
+{
+  if (bytes <= *cap) return true;
+  if (*buf) {
+    cudaStreamSynchronize(t->h->stream);
+    cudaFree(*buf);
+    *buf = nullptr;
+    *cap = 0;
+  }
+  const size_t want = bytes + bytes / 8;
+  if (cudaMalloc(buf, want) != cudaSuccess) {
+    cudaGetLastError();
+    *buf = nullptr;
+    return false;
+  }
+  *cap = want;
+  return true;
 }
 
 size_t align256(size_t b) { return (b + 255) / 256 * 256; }
@@ -169,7 +203,7 @@ hbtu_status hbtu_index_destroy(hbtu_index_table *t)
 {
   if (!t) return HBTU_OK;
   if (t->h) cudaSetDevice(t->h->device);
-  ix_release(t);
+  ix_free(t);
   delete t;
   return HBTU_OK;
 }
@@ -189,24 +223,28 @@ hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int6
   if (n == 0) return HBTU_OK;
   const bool host = location == HBTU_HOST;
   try {
-    // pass 1: key range (one small read back)
-    const size_t bkeys = align256(sizeof(int64_t) * n), bvals = align256(sizeof(int64_t) * n);
-    const size_t bmm = 256;
-    char *stage = nullptr;
-    const size_t bstage = bkeys + bvals + bmm;
-    if (cudaMalloc(&stage, bstage) != cudaSuccess) {
-      cudaGetLastError();
-      return ix_fail(t, HBTU_ERR_OUT_OF_MEMORY, "index fill: staging");
+    if (!t->aux) {
+      if (cudaMalloc(&t->aux, 256) != cudaSuccess) {
+        cudaGetLastError();
+        t->aux = nullptr;
+        return ix_fail(t, HBTU_ERR_OUT_OF_MEMORY, "index fill: small buffer");
+      }
     }
-    int64_t *dkeys = reinterpret_cast<int64_t *>(stage);
-    int64_t *dvals = reinterpret_cast<int64_t *>(stage + bkeys);
-    unsigned long long *mm = reinterpret_cast<unsigned long long *>(stage + bkeys + bvals);
+    unsigned long long *mm = t->aux;
+    int *err = reinterpret_cast<int *>(t->aux + 2);
+    const size_t bkeys = align256(sizeof(int64_t) * n), bvals = align256(sizeof(int64_t) * n);
     const int64_t *ksrc = keys, *vsrc = values;
-    const cudaMemcpyKind kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-    HBTU_CUDA(cudaMemcpyAsync(dkeys, keys, sizeof(int64_t) * n, kind, st));
-    HBTU_CUDA(cudaMemcpyAsync(dvals, values, sizeof(int64_t) * n, kind, st));
-    ksrc = dkeys;
-    vsrc = dvals;
+    if (host) {  // stage the host arrays on the device
+      if (!ix_grow(t, &t->stage, &t->stage_cap, bkeys + bvals))
+        return ix_fail(t, HBTU_ERR_OUT_OF_MEMORY, "index fill: staging");
+      int64_t *dkeys = reinterpret_cast<int64_t *>(t->stage);
+      int64_t *dvals = reinterpret_cast<int64_t *>(t->stage + bkeys);
+      HBTU_CUDA(cudaMemcpyAsync(dkeys, keys, sizeof(int64_t) * n, cudaMemcpyHostToDevice, st));
+      HBTU_CUDA(cudaMemcpyAsync(dvals, values, sizeof(int64_t) * n, cudaMemcpyHostToDevice, st));
+      ksrc = dkeys;
+      vsrc = dvals;
+    }
+    // pass 1: key range (one small read back)
     const unsigned long long init[2] = {~0ull, 0ull};
     HBTU_CUDA(cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, st));
     k_ix_minmax<<<std::min<int64_t>(iblk(n), 152 * 8), kIB, 0, st>>>(ksrc, n, mm);
@@ -219,14 +257,10 @@ hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int6
     const unsigned long long span = (unsigned long long)t->kmax - (unsigned long long)t->kmin + 1ull;
     if (t->flat) {
       if (span == 0ull || span > (1ull << 32)) {
-        cudaFree(stage);
         ix_release(t);
         return ix_fail(t, HBTU_ERR_TOO_LARGE, "flat index: key span above 2^32");
       }
-      const size_t total = bvals + align256(sizeof(int) * span);
-      if (cudaMalloc(&t->mem, total) != cudaSuccess) {
-        cudaGetLastError();
-        cudaFree(stage);
+      if (!ix_grow(t, &t->mem, &t->cap, bvals + align256(sizeof(int) * span))) {
         ix_release(t);
         return ix_fail(t, HBTU_ERR_OUT_OF_MEMORY, "flat index: dense array");
       }
@@ -243,10 +277,7 @@ hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int6
       const size_t b8 = align256(sizeof(unsigned long long) * n), b4 = align256(sizeof(int) * n);
       const size_t bstat = align256(sizeof(unsigned) * sort_status_words(n));
       const size_t bhist = align256(sizeof(unsigned) * 16 * 256);
-      const size_t total = bvals + 2 * b8 + 4 * b4 + bstat + 2 * bhist + 256;
-      if (cudaMalloc(&t->mem, total) != cudaSuccess) {
-        cudaGetLastError();
-        cudaFree(stage);
+      if (!ix_grow(t, &t->mem, &t->cap, bvals + 2 * b8 + 4 * b4 + bstat + 2 * bhist)) {
         ix_release(t);
         return ix_fail(t, HBTU_ERR_OUT_OF_MEMORY, "mapped index: sort buffers");
       }
@@ -271,8 +302,7 @@ hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int6
       sb.os_ghist = reinterpret_cast<unsigned *>(q);
       q += bhist;
       sb.os_goff = reinterpret_cast<unsigned *>(q);
-      q += bhist;
-      sb.error = reinterpret_cast<int *>(q);
+      sb.error = err;
       HBTU_CUDA(cudaMemsetAsync(sb.error, 0, sizeof(int), st));
       HBTU_CUDA(cudaMemcpyAsync(t->values, vsrc, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, st));
       k_ix_prepare<<<iblk(n), kIB, 0, st>>>(ksrc, n, t->kmin, sb.lo_a, sb.hi_a, sb.val_a);
@@ -288,17 +318,14 @@ hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int6
       radix_sort(sb, n, words, shifts, np, st);
       t->skeys = sb.lo_a;
       t->spos = sb.val_a;
-      int err = 0;
-      HBTU_CUDA(cudaMemcpyAsync(&err, sb.error, sizeof(int), cudaMemcpyDeviceToHost, st));
+      int herr = 0;
+      HBTU_CUDA(cudaMemcpyAsync(&herr, sb.error, sizeof(int), cudaMemcpyDeviceToHost, st));
       HBTU_CUDA(cudaStreamSynchronize(st));
-      if (err) {
-        cudaFree(stage);
+      if (herr) {
         ix_release(t);
         return ix_fail(t, HBTU_ERR_CUDA, "mapped index: radix sort look-back");
       }
     }
-    HBTU_CUDA(cudaStreamSynchronize(st));
-    cudaFree(stage);
     t->n = n;
     return HBTU_OK;
   } catch (const CudaError &e) {
@@ -318,17 +345,14 @@ hbtu_status hbtu_index_lookup(hbtu_index_table *t, const int64_t *keys, int64_t 
   cudaSetDevice(h->device);
   cudaStream_t st = h->stream;
   const bool host = location == HBTU_HOST;
-  char *stage = nullptr;
   try {
     const int64_t *dq = keys;
     int64_t *dout = out;
     if (host) {
-      if (cudaMalloc(&stage, 2 * align256(sizeof(int64_t) * m)) != cudaSuccess) {
-        cudaGetLastError();
+      if (!ix_grow(t, &t->stage, &t->stage_cap, 2 * align256(sizeof(int64_t) * m)))
         return ix_fail(t, HBTU_ERR_OUT_OF_MEMORY, "index lookup: staging");
-      }
-      int64_t *sq = reinterpret_cast<int64_t *>(stage);
-      dout = reinterpret_cast<int64_t *>(stage + align256(sizeof(int64_t) * m));
+      int64_t *sq = reinterpret_cast<int64_t *>(t->stage);
+      dout = reinterpret_cast<int64_t *>(t->stage + align256(sizeof(int64_t) * m));
       HBTU_CUDA(cudaMemcpyAsync(sq, keys, sizeof(int64_t) * m, cudaMemcpyHostToDevice, st));
       dq = sq;
     }
@@ -342,11 +366,9 @@ hbtu_status hbtu_index_lookup(hbtu_index_table *t, const int64_t *keys, int64_t 
     if (host) {
       HBTU_CUDA(cudaMemcpyAsync(out, dout, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, st));
       HBTU_CUDA(cudaStreamSynchronize(st));
-      cudaFree(stage);
     }
     return HBTU_OK;
   } catch (const CudaError &e) {
-    if (stage) cudaFree(stage);
     return ix_fail(t, HBTU_ERR_CUDA, e.what.c_str());
   }
 }

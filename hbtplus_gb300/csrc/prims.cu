@@ -201,7 +201,9 @@ constexpr size_t kSmallSortSmem = (size_t)kSmallN * 2 * (8 + 4 + 4);
 // pass over all digits); each tile then finds how many earlier elements
 // share its digit values by decoupled look-back over the tiles before it
 // (tile indices come from an atomic counter, so a tile only waits on tiles
-// that have started), and scatters with the same stable ranks as above.
+// that have started).  The tile is first sorted stably in shared memory,
+// with the same ranks as above, so each digit's run is written out to
+// consecutive addresses.
 // Status words: bits 30-31 flag (1 = tile count, 2 = inclusive prefix),
 // bits 0-29 the count.  Every wait is bounded; a wait that runs out sets
 // *err and the pass continues (results are then wrong and the call fails).
@@ -263,7 +265,12 @@ __global__ void __launch_bounds__(kBlock) k_os_pass(
   __shared__ unsigned wcnt[kBlock / 32][256];
   __shared__ unsigned run_base[256];
   __shared__ unsigned hist[256];
+  __shared__ unsigned toff[256];  // first slot of each digit in the tile's sorted order
   __shared__ unsigned base[256];
+  __shared__ unsigned wsum[kBlock / 32];
+  __shared__ unsigned long long s_lo[kTile];
+  __shared__ unsigned s_hi[kTile];
+  __shared__ int s_val[kTile];
   __shared__ int tile_s;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) tile_s = atomicAdd(tile_counter, 1);
@@ -274,7 +281,7 @@ __global__ void __launch_bounds__(kBlock) k_os_pass(
   __syncthreads();
   const int tile = tile_s;
   const long long t0 = (long long)tile * kTile;
-  // this tile's digits, kept for the scatter
+  // this tile's digits
   unsigned dg[kItems];
 #pragma unroll
   for (int r = 0; r < kItems; r++) {
@@ -286,32 +293,24 @@ __global__ void __launch_bounds__(kBlock) k_os_pass(
     }
   }
   __syncthreads();
-  // publish this tile's counts, then look back for the earlier tiles' total
+  // publish this tile's counts at once, so later tiles can look back past it
   volatile unsigned *st = status;
   const unsigned cnt = hist[tid];
   st[(long long)tile * 256 + tid] = (tile == 0 ? kFlagPre : kFlagAgg) | cnt;
-  unsigned prefix = 0;
-  for (int k = tile - 1; k >= 0;) {
-    const unsigned v = st[(long long)k * 256 + tid];
-    const unsigned flag = v & ~kCountMask;
-    if (flag == 0u) {
-      long long spins = 0;
-      unsigned w = 0;
-      while ((w = st[(long long)k * 256 + tid]) == 0u && ++spins < kSpinLimit) {
-      }
-      if (w == 0u) {  // the earlier tile never published: give up on this pass
-        atomicExch(err, 1);
-        break;
-      }
-      continue;
+  {  // tile-local exclusive offsets of the digits
+    unsigned x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
     }
-    prefix += v & kCountMask;
-    if (flag == kFlagPre) break;
-    k--;
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    unsigned before = 0;
+    for (int w = 0; w < warp; w++) before += wsum[w];
+    toff[tid] = before + x - cnt;
   }
-  if (tile > 0) st[(long long)tile * 256 + tid] = kFlagPre | ((prefix + cnt) & kCountMask);
-  base[tid] = goff[tid] + prefix;
-  __syncthreads();
+  // stable local sort of the tile into shared memory (ranks in element order)
   const unsigned lt = (1u << lane) - 1u;
   for (int r = 0; r < kItems; r++) {
     const long long e = t0 + r * kBlock + tid;
@@ -341,15 +340,49 @@ __global__ void __launch_bounds__(kBlock) k_os_pass(
     }
     __syncthreads();
     if (valid) {
-      const long long dst = (long long)base[d] + wcnt[warp][d] + rank;
-      hi_out[dst] = h;
-      lo_out[dst] = l;
-      val_out[dst] = v;
+      const unsigned slot = toff[d] + wcnt[warp][d] + rank;
+      s_hi[slot] = h;
+      s_lo[slot] = l;
+      s_val[slot] = v;
     }
     __syncthreads();
 #pragma unroll
     for (int w = 0; w < kBlock / 32; w++) wcnt[w][tid] = 0;
     __syncthreads();
+  }
+  // look back for the earlier tiles' total of each digit
+  unsigned prefix = 0;
+  for (int k = tile - 1; k >= 0;) {
+    const unsigned v = st[(long long)k * 256 + tid];
+    const unsigned flag = v & ~kCountMask;
+    if (flag == 0u) {
+      long long spins = 0;
+      unsigned w = 0;
+      while ((w = st[(long long)k * 256 + tid]) == 0u && ++spins < kSpinLimit) {
+      }
+      if (w == 0u) {  // the earlier tile never published: give up on this pass
+        atomicExch(err, 1);
+        break;
+      }
+      continue;
+    }
+    prefix += v & kCountMask;
+    if (flag == kFlagPre) break;
+    k--;
+  }
+  if (tile > 0) st[(long long)tile * 256 + tid] = kFlagPre | ((prefix + cnt) & kCountMask);
+  base[tid] = goff[tid] + prefix;
+  __syncthreads();
+  // write out in sorted order: each digit's run lands contiguously
+  const int tn = (int)min((long long)kTile, n - t0);
+  for (int i = tid; i < tn; i += kBlock) {
+    const unsigned h = s_hi[i];
+    const unsigned long long l = s_lo[i];
+    const unsigned d = rs_digit(h, l, word, shift);
+    const long long dst = (long long)base[d] + (i - (int)toff[d]);
+    hi_out[dst] = h;
+    lo_out[dst] = l;
+    val_out[dst] = s_val[i];
   }
 }
 
