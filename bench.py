@@ -68,6 +68,9 @@ def parse():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--leaf-runs", type=int, default=-1,
                     help="walk_leaf_runs option of the FP32 walk (-1: library default)")
+    ap.add_argument("--walk-schedule", type=int, default=-1,
+                    help="walk_schedule option of the FP32 walk (-1: library default)")
+
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -246,6 +249,7 @@ def config_of(args, batch):
             "max_subhalo": int(np.max(np.diff(batch["offsets"]))),
             "softening": 0.002, "open_angle": args.open_angle, "max_sample_size": 0,
             "precision": args.precision, "walk_leaf_runs": args.leaf_runs if args.leaf_runs >= 0 else 1,
+            "walk_schedule": args.walk_schedule if args.walk_schedule >= 0 else 0,
             "l2": "flushed before each timed step (256 MB write)"}
 
 
@@ -411,6 +415,9 @@ def main():
     ub = U.Unbinder(params, precision=prec, device=local)
     if args.leaf_runs >= 0:
         ub.set_option("walk_leaf_runs", args.leaf_runs)
+    if args.walk_schedule >= 0:
+        ub.set_option("walk_schedule", args.walk_schedule)
+
     stream = torch.cuda.current_stream(dev)
     ub.set_stream(stream.cuda_stream)
 
