@@ -5,8 +5,11 @@
 // particle IDs back into snapshot positions (src/snapshot.h:191-224).
 //   mapped (MappedIndexTable_t): the (key, index) pairs sorted by key, then a
 //     binary search per query; a negative key is absent (hash.tpp:18-55).
-//     Here: a stable radix sort of key - KeyMin (only the digits the key span
-//     needs) and a lower-bound search per query, one thread per query.
+//     Here: an open-addressing hash table in HBM (linear probing, at most half
+//     full, splitmix64 finalizer as the hash) whose slots hold input
+//     positions; one thread per pair claims a slot with a 32-bit atomicCAS
+//     (a duplicate key keeps the smallest position, atomicMin), one thread per
+//     query probes; no sort.  The answers are the sorted table's.
 //   flat (FlatIndexTable_t): a dense array over [KeyMin, KeyMax]
 //     (hash.tpp:59-109).  Here: the position of each pair scattered into the
 //     dense array, one thread per pair.
@@ -29,10 +32,11 @@ struct hbtu_index_table {
   size_t cap = 0;
   char *stage = nullptr;  // host-memory calls: staging of keys, values, queries
   size_t stage_cap = 0;
-  unsigned long long *aux = nullptr;  // key min / max (biased), sort error flag
+  unsigned long long *aux = nullptr;  // key min / max (biased)
   int64_t *values = nullptr;
-  unsigned long long *skeys = nullptr;  // mapped: sorted key - kmin
-  int *spos = nullptr;                  // mapped: input position of each sorted key
+  int64_t *keys = nullptr;   // mapped: the keys, by input position
+  int *hslot = nullptr;      // mapped: input position held by each slot (-1: free)
+  unsigned long long hmask = 0;  // mapped: slots - 1 (a power of two)
   int *dense = nullptr;                 // flat: input position per key - kmin, -1 if none
 };
 
@@ -61,14 +65,36 @@ __global__ void __launch_bounds__(kIB) k_ix_minmax(const int64_t *keys, int64_t 
   }
 }
 
-__global__ void __launch_bounds__(kIB) k_ix_prepare(const int64_t *keys, int64_t n, int64_t kmin,
-                                                    unsigned long long *lo, unsigned *hi, int *pos)
+__device__ __forceinline__ unsigned long long ix_hash(unsigned long long x)
+{  // splitmix64 finalizer (Steele, Lea & Flood 2014)
+  x ^= x >> 30;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27;
+  x *= 0x94d049bb133111ebull;
+  x ^= x >> 31;
+  return x;
+}
+
+// One thread per pair: claim a free slot for the key's position, or, when
+// the key holds a slot already, keep the smaller position there.  Negative
+// keys are absent in the reference's table.
+__global__ void __launch_bounds__(kIB) k_ix_hash_fill(const int64_t *keys, int64_t n, int *hslot,
+                                                      unsigned long long mask)
 {
   const int64_t i = (int64_t)blockIdx.x * kIB + threadIdx.x;
   if (i >= n) return;
-  lo[i] = (unsigned long long)keys[i] - (unsigned long long)kmin;
-  hi[i] = 0u;
-  pos[i] = (int)i;
+  const long long k = keys[i];
+  if (k < 0) return;
+  unsigned long long slot = ix_hash((unsigned long long)k) & mask;
+  for (unsigned long long probe = 0; probe <= mask; probe++) {  // the table is at most half full
+    const int prev = atomicCAS(&hslot[slot], -1, (int)i);
+    if (prev < 0) return;
+    if (keys[prev] == k) {
+      atomicMin(&hslot[slot], (int)i);
+      return;
+    }
+    slot = (slot + 1) & mask;
+  }
 }
 
 __global__ void __launch_bounds__(kIB) k_ix_flat_clear(int *dense, int64_t span)
@@ -86,9 +112,10 @@ __global__ void __launch_bounds__(kIB) k_ix_flat_fill(const int64_t *keys, int64
   atomicMax(&dense[(unsigned long long)keys[i] - (unsigned long long)kmin], (int)i);
 }
 
-__global__ void __launch_bounds__(kIB) k_ix_lookup_mapped(const unsigned long long *skeys,
-                                                          const int *spos, const int64_t *values,
-                                                          int64_t n, int64_t kmin, int64_t kmax,
+__global__ void __launch_bounds__(kIB) k_ix_lookup_mapped(const int64_t *keys, const int *hslot,
+                                                          const int64_t *values,
+                                                          unsigned long long mask, int64_t n,
+                                                          int64_t kmin, int64_t kmax,
                                                           int64_t null_index, const int64_t *q,
                                                           int64_t m, int64_t *out)
 {
@@ -97,16 +124,16 @@ __global__ void __launch_bounds__(kIB) k_ix_lookup_mapped(const unsigned long lo
   const int64_t key = q[j];
   int64_t r = null_index;
   if (key >= 0 && n > 0 && key >= kmin && key <= kmax) {
-    const unsigned long long k = (unsigned long long)key - (unsigned long long)kmin;
-    int64_t lo = 0, hi = n;  // lower bound
-    while (lo < hi) {
-      const int64_t mid = lo + ((hi - lo) >> 1);
-      if (skeys[mid] < k)
-        lo = mid + 1;
-      else
-        hi = mid;
+    unsigned long long slot = ix_hash((unsigned long long)key) & mask;
+    for (unsigned long long probe = 0; probe <= mask; probe++) {
+      const int p = hslot[slot];
+      if (p < 0) break;
+      if (keys[p] == key) {
+        r = values[p];
+        break;
+      }
+      slot = (slot + 1) & mask;
     }
-    if (lo < n && skeys[lo] == k) r = values[spos[lo]];
   }
   out[j] = r;
 }
@@ -139,8 +166,9 @@ hbtu_status ix_fail(hbtu_index_table *t, hbtu_status st, const char *msg)
 void ix_release(hbtu_index_table *t)
 {
   t->values = nullptr;
-  t->skeys = nullptr;
-  t->spos = nullptr;
+  t->keys = nullptr;
+  t->hslot = nullptr;
+  t->hmask = 0;
   t->dense = nullptr;
   t->n = 0;
   t->kmin = 0;
@@ -231,7 +259,6 @@ hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int6
       }
     }
     unsigned long long *mm = t->aux;
-    int *err = reinterpret_cast<int *>(t->aux + 2);
     const size_t bkeys = align256(sizeof(int64_t) * n), bvals = align256(sizeof(int64_t) * n);
     const int64_t *ksrc = keys, *vsrc = values;
     if (host) {  // stage the host arrays on the device
@@ -273,58 +300,24 @@ hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int6
       k_ix_flat_fill<<<iblk(n), kIB, 0, st>>>(ksrc, n, t->kmin, t->dense);
       HBTU_LAUNCHED();
     } else {
-      // sort buffers (two copies of key / subhalo word / payload) + onesweep state
-      const size_t b8 = align256(sizeof(unsigned long long) * n), b4 = align256(sizeof(int) * n);
-      const size_t bstat = align256(sizeof(unsigned) * sort_status_words(n));
-      const size_t bhist = align256(sizeof(unsigned) * 16 * 256);
-      if (!ix_grow(t, &t->mem, &t->cap, bvals + 2 * b8 + 4 * b4 + bstat + 2 * bhist)) {
+      // hash slots: a power of two at least twice the pairs
+      unsigned long long slots = 1024;
+      while (slots < 2ull * (unsigned long long)n) slots <<= 1;
+      const size_t bs = align256(sizeof(int) * slots);
+      if (!ix_grow(t, &t->mem, &t->cap, bvals + bkeys + bs)) {
         ix_release(t);
-        return ix_fail(t, HBTU_ERR_OUT_OF_MEMORY, "mapped index: sort buffers");
+        return ix_fail(t, HBTU_ERR_OUT_OF_MEMORY, "mapped index: hash slots");
       }
-      char *q = t->mem;
-      t->values = reinterpret_cast<int64_t *>(q);
-      q += bvals;
-      SortBuffers sb;
-      sb.lo_a = reinterpret_cast<unsigned long long *>(q);
-      q += b8;
-      sb.lo_b = reinterpret_cast<unsigned long long *>(q);
-      q += b8;
-      sb.hi_a = reinterpret_cast<unsigned *>(q);
-      q += b4;
-      sb.hi_b = reinterpret_cast<unsigned *>(q);
-      q += b4;
-      sb.val_a = reinterpret_cast<int *>(q);
-      q += b4;
-      sb.val_b = reinterpret_cast<int *>(q);
-      q += b4;
-      sb.os_status = reinterpret_cast<unsigned *>(q);
-      q += bstat;
-      sb.os_ghist = reinterpret_cast<unsigned *>(q);
-      q += bhist;
-      sb.os_goff = reinterpret_cast<unsigned *>(q);
-      sb.error = err;
-      HBTU_CUDA(cudaMemsetAsync(sb.error, 0, sizeof(int), st));
+      t->values = reinterpret_cast<int64_t *>(t->mem);
+      t->keys = reinterpret_cast<int64_t *>(t->mem + bvals);
+      t->hslot = reinterpret_cast<int *>(t->mem + bvals + bkeys);
+      t->hmask = slots - 1;
       HBTU_CUDA(cudaMemcpyAsync(t->values, vsrc, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, st));
-      k_ix_prepare<<<iblk(n), kIB, 0, st>>>(ksrc, n, t->kmin, sb.lo_a, sb.hi_a, sb.val_a);
+      HBTU_CUDA(cudaMemcpyAsync(t->keys, ksrc, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, st));
+      HBTU_CUDA(cudaMemsetAsync(t->hslot, 0xff, sizeof(int) * slots, st));  // -1: free
+      k_ix_hash_fill<<<iblk(n), kIB, 0, st>>>(t->keys, n, t->hslot, t->hmask);
       HBTU_LAUNCHED();
-      // only the digits the key span needs
-      int bits = 0;
-      while (bits < 64 && ((span - 1ull) >> bits) != 0ull) bits++;
-      int words[8], shifts[8], np = 0;
-      for (int b = 0; b < bits; b += 8) {
-        words[np] = 0;
-        shifts[np++] = b;
-      }
-      radix_sort(sb, n, words, shifts, np, st);
-      t->skeys = sb.lo_a;
-      t->spos = sb.val_a;
-      int herr = 0;
-      HBTU_CUDA(cudaMemcpyAsync(&herr, sb.error, sizeof(int), cudaMemcpyDeviceToHost, st));
       HBTU_CUDA(cudaStreamSynchronize(st));
-      if (herr) {
-        ix_release(t);
-        return ix_fail(t, HBTU_ERR_CUDA, "mapped index: radix sort look-back");
-      }
     }
     t->n = n;
     return HBTU_OK;
@@ -360,8 +353,8 @@ hbtu_status hbtu_index_lookup(hbtu_index_table *t, const int64_t *keys, int64_t 
       k_ix_lookup_flat<<<iblk(m), kIB, 0, st>>>(t->dense, t->values, t->n, t->kmin, t->kmax,
                                                 t->null_index, dq, m, dout);
     else
-      k_ix_lookup_mapped<<<iblk(m), kIB, 0, st>>>(t->skeys, t->spos, t->values, t->n, t->kmin,
-                                                  t->kmax, t->null_index, dq, m, dout);
+      k_ix_lookup_mapped<<<iblk(m), kIB, 0, st>>>(t->keys, t->hslot, t->values, t->hmask, t->n,
+                                                  t->kmin, t->kmax, t->null_index, dq, m, dout);
     HBTU_LAUNCHED();
     if (host) {
       HBTU_CUDA(cudaMemcpyAsync(out, dout, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, st));

@@ -312,8 +312,9 @@ hbtu_status hbtu_merge_detect(hbtu_handle *h, const hbtu_particles *p, int64_t n
  * ParticleSnapshot_t, src/snapshot.h:191-224, and queried by GetIndex /
  * GetIndices, src/hash.tpp:47-55 / src/hash_remote.tpp:5-99).  A table lives
  * on the handle's device and uses its stream.
- *   flat = 0: MappedIndexTable_t -- pairs sorted by key, binary search per
- *             query; a negative key is absent;
+ *   flat = 0: MappedIndexTable_t (pairs sorted by key, binary search per
+ *             query; a negative key is absent) -- here a hash table with the
+ *             same answers, no sort;
  *   flat = 1: FlatIndexTable_t -- a dense array over [KeyMin, KeyMax] (key
  *             spans above 2^32 are refused: HBTU_ERR_TOO_LARGE).
  * Duplicate keys (undefined in the reference): the first pair in input order
