@@ -1,6 +1,7 @@
 """Particle-ID -> index tables on the GPU, mirroring the reference's
-IndexTable_t (src/hash.h:47-112): MappedIndexTable_t (sorted pairs, binary
-search) and FlatIndexTable_t (dense array over the key range).
+IndexTable_t (src/hash.h:47-112): MappedIndexTable_t (the reference's sorted
+pairs and binary search; a hash table here, same answers) and
+FlatIndexTable_t (dense array over the key range).
 
     with Unbinder(params) as ub:
         table = MappedIndexTable(ub)              # or FlatIndexTable(ub)
@@ -91,7 +92,8 @@ class _IndexTable:
 
 
 class MappedIndexTable(_IndexTable):
-    """MappedIndexTable_t (src/hash.tpp:18-55): sorted pairs, binary search."""
+    """MappedIndexTable_t (src/hash.tpp:18-55): the reference sorts the pairs
+    and binary-searches them; here a GPU hash table with the same answers."""
     _flat = 0
 
 
