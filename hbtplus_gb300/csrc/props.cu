@@ -11,8 +11,9 @@
 //     floored at the softening, v^2 = m / r and its first maximum, the
 //     half-mass and 95.5% radii, and the outermost radius inside which the
 //     mean density exceeds 200 times critical;
-//   shape: the inertia tensors, float terms summed in double per 1024-particle
-//     chunk in a fixed order, then over the chunks in order.
+//   shape: the inertia tensors, float terms summed in double per 256-particle
+//     chunk (one warp: lane-strided sums, then a fixed shuffle tree), then over
+//     the chunks in order.
 // Exactness.  The reference sums the cumulative mass sequentially in double.
 // Here it is summed exactly in 64-bit fixed point (units of the lowest mass
 // bit of the batch), which equals the sequential double sum whenever that sum
@@ -37,7 +38,7 @@ namespace hbtu {
 namespace {
 
 constexpr int kPB = 256;
-constexpr int kPChunk = 1024;
+constexpr int kPChunk = 256;  // shape particles per warp-chunk
 constexpr long long kExact = 1ll << 53;
 
 struct PropSeg {
@@ -103,32 +104,41 @@ __device__ __forceinline__ float periodic_distance(const float x[3], const float
   return __fsqrt_rn(fadd(fadd(fmul(d[0], d[0]), fmul(d[1], d[1])), fmul(d[2], d[2])));
 }
 
-// Per bound element: distance, sort record, binary range of the masses.
+// Per bound element: distance, sort record, binary range of the masses (the
+// range reduced over the warp before its one atomic).
 __global__ void __launch_bounds__(kPB) k_pr_elem(const PropSeg *seg, const int64_t *boff, int S,
                                                  int64_t T, const float *pos, const float *mass,
                                                  const int64_t *order, unsigned long long *lo,
                                                  unsigned *hi, int *val, int *flags, DevParams P)
 {
   const int64_t j = (int64_t)blockIdx.x * kPB + threadIdx.x;
-  if (j >= T) return;
-  const int s = seg_of(boff, S, j);
-  const PropSeg g = seg[s];
-  const int64_t o = order[g.off + (j - g.boff)];
-  if (o < 0 || o >= g.n) atomicOr(&flags[F_ORDER], 1);
-  const int64_t pid = bound_particle(g, order, j - g.boff, g.n);
-  const float x[3] = {pos[3 * pid], pos[3 * pid + 1], pos[3 * pid + 2]};
-  const float r = periodic_distance(x, g.cen, P);
-  lo[j] = (unsigned long long)__float_as_uint(r);  // r >= 0: bits sort as values
-  hi[j] = (unsigned)s;
-  val[j] = (int)j;
-  const unsigned b = __float_as_uint(mass[pid]);
-  const int ex = (int)((b >> 23) & 255u);
-  const unsigned m = ex ? ((b & 0x7fffffu) | 0x800000u) : (b & 0x7fffffu);
-  if (((b >> 31) && (b & 0x7fffffffu)) || ex == 255) atomicOr(&flags[F_NEG], 1);
-  if (m && ex != 255) {
-    const int e0 = (ex ? ex : 1) - 150;  // value = m * 2^e0
-    atomicMin(&flags[F_LOW], e0 + __ffs(m) - 1);
-    atomicMax(&flags[F_HIGH], e0 + 31 - __clz(m));
+  int lowbit = 0x7fffffff, highbit = -0x7fffffff;
+  if (j < T) {
+    const int s = seg_of(boff, S, j);
+    const PropSeg g = seg[s];
+    const int64_t o = order[g.off + (j - g.boff)];
+    if (o < 0 || o >= g.n) atomicOr(&flags[F_ORDER], 1);
+    const int64_t pid = bound_particle(g, order, j - g.boff, g.n);
+    const float x[3] = {pos[3 * pid], pos[3 * pid + 1], pos[3 * pid + 2]};
+    const float r = periodic_distance(x, g.cen, P);
+    lo[j] = (unsigned long long)__float_as_uint(r);  // r >= 0: bits sort as values
+    hi[j] = (unsigned)s;
+    val[j] = (int)j;
+    const unsigned b = __float_as_uint(mass[pid]);
+    const int ex = (int)((b >> 23) & 255u);
+    const unsigned m = ex ? ((b & 0x7fffffu) | 0x800000u) : (b & 0x7fffffu);
+    if (((b >> 31) && (b & 0x7fffffffu)) || ex == 255) atomicOr(&flags[F_NEG], 1);
+    if (m && ex != 255) {
+      const int e0 = (ex ? ex : 1) - 150;  // value = m * 2^e0
+      lowbit = e0 + __ffs(m) - 1;
+      highbit = e0 + 31 - __clz(m);
+    }
+  }
+  lowbit = __reduce_min_sync(0xffffffffu, lowbit);
+  highbit = __reduce_max_sync(0xffffffffu, highbit);
+  if ((threadIdx.x & 31) == 0 && lowbit != 0x7fffffff) {
+    atomicMin(&flags[F_LOW], lowbit);
+    atomicMax(&flags[F_HIGH], highbit);
   }
 }
 
@@ -180,8 +190,23 @@ __global__ void k_pr_seq(const PropSeg *__restrict__ seg, int S, int64_t T,
   }
 }
 
+// Maximum over the lanes of each run of equal s (runs are contiguous: the
+// elements are sorted by subhalo), left in the run's first lane.
+__device__ __forceinline__ unsigned long long run_max(unsigned long long v, int s)
+{
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+    const int ws = __shfl_down_sync(0xffffffffu, s, o);
+    if (lane + o < 32 && ws == s) v = max(v, w);
+  }
+  return v;
+}
+
 // Per sorted element: cumulative mass, floored radius, v^2, the per-subhalo
-// first maximum, the overdensity radius and the two quantile radii.
+// first maximum, the overdensity radius and the two quantile radii.  The
+// maxima are reduced over each warp's runs of one subhalo before the atomics.
 __global__ void __launch_bounds__(kPB) k_pr_prof(const PropSeg *seg, const int64_t *boff, int S,
                                                  int64_t T, const unsigned long long *rsorted,
                                                  const long long *mfix, const long long *cum,
@@ -190,43 +215,57 @@ __global__ void __launch_bounds__(kPB) k_pr_prof(const PropSeg *seg, const int64
                                                  long long *so, float *quant)
 {
   const int64_t q = (int64_t)blockIdx.x * kPB + threadIdx.x;
-  if (q >= T) return;
-  const int s = seg_of(boff, S, q);  // sorted by subhalo first: the same ranges
-  const PropSeg g = seg[s];
-  const int64_t k = q - g.boff;
-  int K;
-  const bool scaled = fix_scale(flags, T, &K);
-  float m;
-  if (seg_exact(g, cum, scaled))
-    m = d2f(ldexp((double)(cum[q] + mfix[q] - cum[g.boff]), -K));  // exact below 2^53
-  else
-    m = mc[q];
-  float r = __uint_as_float((unsigned)rsorted[q]);
-  if (r < eps) r = eps;
-  const float v = __fdiv_rn(m, r);
-  rc[q] = r;
-  mc[q] = m;
-  atomicMax(&vmax[s], ((unsigned long long)__float_as_uint(v) << 32) |
-                          (unsigned long long)(0xffffffffu - (unsigned)k));
-  if (m > fmul(fmul(fmul(rho_vir, r), r), r)) atomicMax(&so[s], (long long)k);
-  if (k == g.nb / 2) quant[2 * s] = r;
-  if (k == (int64_t)((double)g.nb * 0.955)) quant[2 * s + 1] = r;
+  const int lane = threadIdx.x & 31;
+  int s = -1 - lane;  // a run of its own for lanes past the end
+  unsigned long long vkey = 0ull, sokey = 0ull;  // so index + 1, 0: none
+  if (q < T) {
+    s = seg_of(boff, S, q);  // sorted by subhalo first: the same ranges
+    const PropSeg g = seg[s];
+    const int64_t k = q - g.boff;
+    int K;
+    const bool scaled = fix_scale(flags, T, &K);
+    float m;
+    if (seg_exact(g, cum, scaled))
+      m = d2f(ldexp((double)(cum[q] + mfix[q] - cum[g.boff]), -K));  // exact below 2^53
+    else
+      m = mc[q];
+    float r = __uint_as_float((unsigned)rsorted[q]);
+    if (r < eps) r = eps;
+    const float v = __fdiv_rn(m, r);
+    rc[q] = r;
+    mc[q] = m;
+    vkey = ((unsigned long long)__float_as_uint(v) << 32) |
+           (unsigned long long)(0xffffffffu - (unsigned)k);
+    if (m > fmul(fmul(fmul(rho_vir, r), r), r)) sokey = (unsigned long long)k + 1ull;
+    if (k == g.nb / 2) quant[2 * s] = r;
+    if (k == (int64_t)((double)g.nb * 0.955)) quant[2 * s + 1] = r;
+  }
+  vkey = run_max(vkey, s);
+  sokey = run_max(sokey, s);
+  const int prev = __shfl_up_sync(0xffffffffu, s, 1);
+  if (q < T && (lane == 0 || prev != s)) {
+    atomicMax(&vmax[s], vkey);
+    if (sokey) atomicMax(&so[s], (long long)sokey - 1);
+  }
 }
 
-// Shape: the 12 tensor sums of one 1024-particle chunk (particles 1 .. Nbound-1
-// in bound order), each thread over a strided subset, then the block in order.
-__global__ void __launch_bounds__(kPB) k_pr_shape(const PropSeg *seg, const int *chunk_seg,
+// Shape: the 12 tensor sums of one 256-particle chunk (particles 1 .. Nbound-1
+// in bound order) per warp: each lane over a strided subset, then a fixed
+// shuffle tree; eight chunks per block.
+__global__ void __launch_bounds__(kPB) k_pr_shape(const PropSeg *seg, const int *chunk_seg, int nch,
                                                   const float *pos, const float *mass,
                                                   const int64_t *order, double *csum, DevParams P)
 {
-  const int b = blockIdx.x;
+  const int b = (int)(((int64_t)blockIdx.x * kPB + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (b >= nch) return;  // whole warps leave together
   const int s = chunk_seg[b];
   const PropSeg g = seg[s];
   const int64_t lo = 1 + (int64_t)(b - g.chunk0) * kPChunk;
   const int64_t hi = min(lo + kPChunk, g.nb);
   double v[12];
   for (int k = 0; k < 12; k++) v[k] = 0.;
-  for (int64_t i = lo + threadIdx.x; i < hi; i += kPB) {
+  for (int64_t i = lo + lane; i < hi; i += 32) {
     const int64_t pid = bound_particle(g, order, i, g.n);
     const float m = mass[pid];
     float dx = fsub(pos[3 * pid], g.cen[0]), dy = fsub(pos[3 * pid + 1], g.cen[1]),
@@ -251,13 +290,15 @@ __global__ void __launch_bounds__(kPB) k_pr_shape(const PropSeg *seg, const int 
     v[10] = dadd(v[10], f2d(__fdiv_rn(fmul(dy, dz), dr2)));
     v[11] = dadd(v[11], f2d(__fdiv_rn(dz2, dr2)));
   }
-  __shared__ double sh[12][kPB];
-  for (int k = 0; k < 12; k++) sh[k][threadIdx.x] = v[k];
-  __syncthreads();
-  if (threadIdx.x < 12) {
-    double t = 0.;
-    for (int j = 0; j < kPB; j++) t = dadd(t, sh[threadIdx.x][j]);
-    csum[(size_t)b * 12 + threadIdx.x] = t;
+#pragma unroll
+  for (int k = 0; k < 12; k++)
+    for (int o = 16; o > 0; o >>= 1) v[k] = dadd(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+  if (lane < 12) {
+    double t = v[0];
+#pragma unroll
+    for (int k = 1; k < 12; k++)
+      if (lane == k) t = v[k];
+    csum[(size_t)b * 12 + lane] = t;
   }
 }
 
@@ -506,7 +547,8 @@ extern "C" hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_partic
       HBTU_LAUNCHED();
     }
     if (nch) {
-      k_pr_shape<<<nch, kPB, 0, st>>>(d_seg, d_cseg, d_pos, d_mass, d_ord, d_csum, P);
+      k_pr_shape<<<(unsigned)((32 * (int64_t)nch + kPB - 1) / kPB), kPB, 0, st>>>(
+          d_seg, d_cseg, nch, d_pos, d_mass, d_ord, d_csum, P);
       HBTU_LAUNCHED();
     }
     k_pr_final<<<(unsigned)((32 * nsub + 127) / 128), 128, 0, st>>>(
