@@ -293,11 +293,13 @@ __global__ void __launch_bounds__(kWB) k_walk_fp32(Ctx c, int total)
 // The reference's opening decision in double, for a target whose float test
 // fell within 1e-5 of the threshold.  Not inlined: the compiler would
 // otherwise evaluate the double arithmetic on every step and select.
-__device__ __noinline__ bool exact_open(float4 na, const float q[3], float l2, double th2d)
+// The target position comes by value, so the walk keeps it in registers.
+__device__ __noinline__ bool exact_open(float4 na, float qx, float qy, float qz, float l2,
+                                        double th2d)
 {
-  const double ex = dsub((double)na.x, (double)q[0]);
-  const double ey = dsub((double)na.y, (double)q[1]);
-  const double ez = dsub((double)na.z, (double)q[2]);
+  const double ex = dsub((double)na.x, (double)qx);
+  const double ey = dsub((double)na.y, (double)qy);
+  const double ez = dsub((double)na.z, (double)qz);
   const double er2 = dadd(dadd(dmul(ex, ex), dmul(ey, ey)), dmul(ez, ez));
   return (double)l2 > dmul(er2, th2d);
 }
@@ -327,7 +329,8 @@ __global__ void __launch_bounds__(kB) k_walk_fp32_lean(Ctx c, int total)
     const float r2 = dist2(na, t.q);
     const float lo = __int_as_float(nm.z), up = __int_as_float(nm.w);
     bool open = r2 < lo;
-    if (r2 >= lo && r2 <= up) open = exact_open(na, t.q, __int_as_float(nm.x & 0x7fffffff), th2d);
+    if (r2 >= lo && r2 <= up)
+      open = exact_open(na, t.q[0], t.q[1], t.q[2], __int_as_float(nm.x & 0x7fffffff), th2d);
     const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
     const float mass = fabsf(na.w);
     float contrib = -mass * rinv;
