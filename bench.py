@@ -68,6 +68,9 @@ def parse():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--leaf-runs", type=int, default=-1,
                     help="walk_leaf_runs option of the FP32 walk (-1: library default)")
+    ap.add_argument("--max-sample", type=int, default=0,
+                    help="MaxSampleSizeOfPotentialEstimate: 0 exact (parity, the default), "
+                         "1000 the reference's production default")
     ap.add_argument("--walk-schedule", type=int, default=-1,
                     help="walk_schedule option of the FP32 walk (-1: library default)")
 
@@ -83,9 +86,10 @@ def dist_env():
     return ws, rank, local
 
 
-def workload(nsub: int, rank: int, kind: str = "batch", theta: float = 0.45):
+def workload(nsub: int, rank: int, kind: str = "batch", theta: float = 0.45,
+             max_sample: int = 0):
     from hbtplus_gb300 import synthetic as S
-    p = S.default_params(open_angle=theta)
+    p = S.default_params(open_angle=theta, max_sample_size=max_sample)
     if kind == "single":
         return S.concat([S.single_subhalo(seed=20261203 + 1000 * rank)]), p
     if kind == "host2e7":
@@ -207,7 +211,7 @@ def run_reference_arm(args, ws, rank):
                           f"the {args.workload} workload has no CPU reference run: one pass "
                           "of the reference over it takes minutes on the host"}), flush=True)
         return
-    batch, params = workload(args.nsub, 0, args.workload, args.open_angle)
+    batch, params = workload(args.nsub, 0, args.workload, args.open_angle, args.max_sample)
     threads = cpu_threads()
     for _ in range(args.warmup):
         cpu_reference_time(params, batch, threads)
@@ -247,7 +251,8 @@ def config_of(args, batch):
     return {"workload": name,
             "nsub": nsub, "particles": int(batch["offsets"][-1]),
             "max_subhalo": int(np.max(np.diff(batch["offsets"]))),
-            "softening": 0.002, "open_angle": args.open_angle, "max_sample_size": 0,
+            "softening": 0.002, "open_angle": args.open_angle,
+            "max_sample_size": args.max_sample,
             "precision": args.precision, "walk_leaf_runs": args.leaf_runs if args.leaf_runs >= 0 else 1,
             "walk_schedule": args.walk_schedule if args.walk_schedule >= 0 else 0,
             "l2": "flushed before each timed step (256 MB write)"}
@@ -408,7 +413,7 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    batch, params = workload(args.nsub, rank, args.workload, args.open_angle)
+    batch, params = workload(args.nsub, rank, args.workload, args.open_angle, args.max_sample)
     nsub = len(batch["offsets"]) - 1
     ntot = int(batch["offsets"][-1])
     prec = 1 if args.precision == "fp64" else 0
