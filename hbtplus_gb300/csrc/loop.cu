@@ -47,8 +47,12 @@ __device__ void block_sum(double (&v)[K], double *out)
 }
 
 // Exclusive scan over segments of up to 4 counters, one block of 1024 threads.
-__device__ void plan_scan4(int S, int (*getter)(const Ctx &, int, int *), const Ctx &c,
-                           int *out0, int *out1, int *out2, int *out3, int *tot)
+// The getter is a template argument so it inlines: each thread's segments are
+// then read with independent loads in flight (an indirect call per segment
+// serialises them).
+template <int (*getter)(const Ctx &, int, int *)>
+__device__ void plan_scan4(int S, const Ctx &c, int *out0, int *out1, int *out2, int *out3,
+                           int *tot)
 {
   __shared__ int wsum[4][kPlanThreads / 32];
   const int per = (S + kPlanThreads - 1) / kPlanThreads;
@@ -204,7 +208,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode)
     }
     __syncthreads();
     if (threadIdx.x == 0) c.plan->inter_done = (long long)inter;
-    plan_scan4(c.S, get_pass, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
+    plan_scan4<get_pass>(c.S, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
     if (threadIdx.x == 0) {
       c.plan->nactive = nact;
       c.plan->ntree_total = tot[0];
@@ -213,20 +217,20 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode)
       c.plan->max_levels = 0;
     }
     __syncthreads();
-    plan_scan4(c.S, get_targets_sorted, c, c.tgt_base, nullptr, nullptr, nullptr, tot);
+    plan_scan4<get_targets_sorted>(c.S, c, c.tgt_base, nullptr, nullptr, nullptr, tot);
     if (threadIdx.x == 0) c.plan->ntgt_total = tot[0];
   } else if (mode == 1) {
-    plan_scan4(c.S, get_bound, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
+    plan_scan4<get_bound>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
     if (threadIdx.x == 0) c.plan->nchunks_bound = tot[0];
   } else if (mode == 2) {
-    plan_scan4(c.S, get_final, c, c.bchunk_base, c.ub_base, nullptr, nullptr, tot);
+    plan_scan4<get_final>(c.S, c, c.bchunk_base, c.ub_base, nullptr, nullptr, tot);
     if (threadIdx.x == 0) {
       c.plan->nchunks_bound = tot[0];
       c.plan->nsort_total = tot[1];
       c.plan->nrefine = tot[2];
     }
   } else {
-    plan_scan4(c.S, get_refine, c, c.ub_base, nullptr, nullptr, nullptr, tot);
+    plan_scan4<get_refine>(c.S, c, c.ub_base, nullptr, nullptr, nullptr, tot);
     if (threadIdx.x == 0) c.plan->nsort_total = tot[0];
   }
 }
@@ -780,7 +784,7 @@ __device__ int get_all_chunks(const Ctx &c, int s, int *v)
 __global__ void __launch_bounds__(kPlanThreads) k_plan_all(Ctx c)
 {
   __shared__ int tot[4];
-  plan_scan4(c.S, get_all_chunks, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
+  plan_scan4<get_all_chunks>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
 }
 
 }  // namespace
