@@ -59,6 +59,9 @@ static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
   c.tchunk_base = cv.take<int>(S + 1);
   c.bchunk_base = cv.take<int>(S + 1);
   c.ub_base = cv.take<int>(S + 1);
+  c.plan_cnt = cv.take<int4>(S);
+  c.plan_cnt2 = cv.take<int4>(S);
+  c.plan_inter = cv.take<long long>(S);
   c.part_info = cv.take<int>(8 * S);
   c.chunk_bbox = cv.take<unsigned>(6 * maxchunks);
   c.chunk_sums = cv.take<double>(24 * maxchunks);

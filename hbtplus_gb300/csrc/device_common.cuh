@@ -151,6 +151,8 @@ struct Ctx {
   PassPlan *plan, *plan_host;
   int *tree_base, *tgt_base;                 // S+1 each
   int *tchunk_base, *bchunk_base, *ub_base;  // S+1 each
+  int4 *plan_cnt, *plan_cnt2;                // S each: gathered plan counters
+  long long *plan_inter;                     // S: gathered interaction counts
   int *seg_off;                              // S+1
   int *seg_order;                            // S: subhaloes by size, largest first
   int opt_leaf_runs;                         // warp schedule streams all-particle cells

@@ -183,7 +183,58 @@ __device__ int get_refine(const Ctx &c, int s, int *v)
   return 0;
 }
 
-__global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode)
+// Large batches: the per-subhalo counters are first gathered into dense
+// arrays by a grid of threads, so the one-block scans read them coalesced
+// (read from the subhalo records, one block's loads serialise on one SM).
+constexpr int kPlanGatherMin = 4096;
+
+template <int (*getter)(const Ctx &, int, int *)>
+__device__ __forceinline__ int4 counts_of(const Ctx &c, int s)
+{
+  int v[4];
+  getter(c, s, v);
+  return make_int4(v[0], v[1], v[2], v[3]);
+}
+
+__global__ void k_plan_gather(Ctx c, int mode)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= c.S) return;
+  if (mode == 0) {
+    c.plan_cnt[s] = counts_of<get_pass>(c, s);
+    int4 t = counts_of<get_targets_sorted>(c, s);  // by position in size order
+    t.y = c.seg[s].status == SEG_ACTIVE;           // summed only
+    c.plan_cnt2[s] = t;
+    c.plan_inter[s] = c.seg[s].interactions;
+  } else if (mode == 1) {
+    c.plan_cnt[s] = counts_of<get_bound>(c, s);
+  } else if (mode == 2) {
+    c.plan_cnt[s] = counts_of<get_final>(c, s);
+  } else {
+    c.plan_cnt[s] = counts_of<get_refine>(c, s);
+  }
+}
+
+__device__ int get_cnt(const Ctx &c, int s, int *v)
+{
+  const int4 q = c.plan_cnt[s];
+  v[0] = q.x;
+  v[1] = q.y;
+  v[2] = q.z;
+  v[3] = q.w;
+  return 0;
+}
+__device__ int get_cnt2(const Ctx &c, int s, int *v)
+{
+  const int4 q = c.plan_cnt2[s];
+  v[0] = q.x;
+  v[1] = q.y;
+  v[2] = q.z;
+  v[3] = q.w;
+  return 0;
+}
+
+__global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode, int gathered)
 {
   __shared__ int tot[4];
   __shared__ int nact;
@@ -196,8 +247,12 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode)
     int cnt = 0;
     unsigned long long it = 0;
     for (int s = threadIdx.x; s < c.S; s += kPlanThreads) {
-      cnt += c.seg[s].status == SEG_ACTIVE;
-      it += (unsigned long long)c.seg[s].interactions;
+      if (gathered) {
+        it += (unsigned long long)c.plan_inter[s];
+      } else {
+        cnt += c.seg[s].status == SEG_ACTIVE;
+        it += (unsigned long long)c.seg[s].interactions;
+      }
     }
     // warp sums first: one shared atomic per warp, not per thread
     cnt = __reduce_add_sync(0xffffffffu, cnt);
@@ -208,29 +263,51 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode)
     }
     __syncthreads();
     if (threadIdx.x == 0) c.plan->inter_done = (long long)inter;
-    plan_scan4<get_pass>(c.S, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
+    if (gathered)
+      plan_scan4<get_cnt>(c.S, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
+    else
+      plan_scan4<get_pass>(c.S, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
     if (threadIdx.x == 0) {
-      c.plan->nactive = nact;
       c.plan->ntree_total = tot[0];
       c.plan->nchunks_tree = tot[1];
       c.plan->nsort_total = tot[3];
       c.plan->max_levels = 0;
     }
     __syncthreads();
-    plan_scan4<get_targets_sorted>(c.S, c, c.tgt_base, nullptr, nullptr, nullptr, tot);
-    if (threadIdx.x == 0) c.plan->ntgt_total = tot[0];
+    if (gathered) {
+      plan_scan4<get_cnt2>(c.S, c, c.tgt_base, nullptr, nullptr, nullptr, tot);
+      if (threadIdx.x == 0) {
+        c.plan->ntgt_total = tot[0];
+        c.plan->nactive = tot[1];
+      }
+    } else {
+      plan_scan4<get_targets_sorted>(c.S, c, c.tgt_base, nullptr, nullptr, nullptr, tot);
+      if (threadIdx.x == 0) {
+        c.plan->ntgt_total = tot[0];
+        c.plan->nactive = nact;
+      }
+    }
   } else if (mode == 1) {
-    plan_scan4<get_bound>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
+    if (gathered)
+      plan_scan4<get_cnt>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
+    else
+      plan_scan4<get_bound>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
     if (threadIdx.x == 0) c.plan->nchunks_bound = tot[0];
   } else if (mode == 2) {
-    plan_scan4<get_final>(c.S, c, c.bchunk_base, c.ub_base, nullptr, nullptr, tot);
+    if (gathered)
+      plan_scan4<get_cnt>(c.S, c, c.bchunk_base, c.ub_base, nullptr, nullptr, tot);
+    else
+      plan_scan4<get_final>(c.S, c, c.bchunk_base, c.ub_base, nullptr, nullptr, tot);
     if (threadIdx.x == 0) {
       c.plan->nchunks_bound = tot[0];
       c.plan->nsort_total = tot[1];
       c.plan->nrefine = tot[2];
     }
   } else {
-    plan_scan4<get_refine>(c.S, c, c.ub_base, nullptr, nullptr, nullptr, tot);
+    if (gathered)
+      plan_scan4<get_cnt>(c.S, c, c.ub_base, nullptr, nullptr, nullptr, tot);
+    else
+      plan_scan4<get_refine>(c.S, c, c.ub_base, nullptr, nullptr, nullptr, tot);
     if (threadIdx.x == 0) c.plan->nsort_total = tot[0];
   }
 }
@@ -811,7 +888,12 @@ void launch_init(Ctx &c, const float *pos, const float *vel, const float *mass,
 
 void launch_plan(Ctx &c, int mode)
 {
-  k_plan<<<1, kPlanThreads, 0, c.st>>>(c, mode);
+  const int gathered = c.S >= kPlanGatherMin;
+  if (gathered) {
+    k_plan_gather<<<nblk(c.S, 256), 256, 0, c.st>>>(c, mode);
+    HBTU_LAUNCHED();
+  }
+  k_plan<<<1, kPlanThreads, 0, c.st>>>(c, mode, gathered);
   HBTU_LAUNCHED();
 }
 
