@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--max-sample", type=int, default=0,
                     help="MaxSampleSizeOfPotentialEstimate: 0 exact (parity, the default), "
                          "1000 the reference's production default")
+    ap.add_argument("--walk-layout", type=int, default=-1,
+                    help="walk_layout option of the FP32 walk (-1: library default)")
     ap.add_argument("--walk-schedule", type=int, default=-1,
                     help="walk_schedule option of the FP32 walk (-1: library default)")
 
@@ -255,6 +257,7 @@ def config_of(args, batch):
             "max_sample_size": args.max_sample,
             "precision": args.precision, "walk_leaf_runs": args.leaf_runs if args.leaf_runs >= 0 else 1,
             "walk_schedule": args.walk_schedule if args.walk_schedule >= 0 else 0,
+            "walk_layout": args.walk_layout if args.walk_layout >= 0 else 1,
             "l2": "flushed before each timed step (256 MB write)"}
 
 
@@ -422,6 +425,8 @@ def main():
         ub.set_option("walk_leaf_runs", args.leaf_runs)
     if args.walk_schedule >= 0:
         ub.set_option("walk_schedule", args.walk_schedule)
+    if args.walk_layout >= 0:
+        ub.set_option("walk_layout", args.walk_layout)
 
     stream = torch.cuda.current_stream(dev)
     ub.set_stream(stream.cuda_stream)

@@ -37,7 +37,7 @@ struct Carver {
   }
 };
 
-static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
+static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S, bool sibling)
 {
   const long long maxchunks = N / kChunk + S + 2;
   c.pm = cv.take<float4>(N);
@@ -98,6 +98,17 @@ static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
   // one spare slot: the walk prefetches node cur+1 speculatively
   c.nd_abs = cv.take<float4>(2 * N + 1);
   c.nd = cv.take<WNode>(2 * N + 1);
+  if (sibling) {  // the FP32 walk's copy of the nodes with each cell's children adjacent
+    c.nd2 = cv.take<WNode>(2 * N + 1);
+    c.newidx = cv.take<int>(2 * N + 1);
+    c.X2 = cv.take<long long>(2 * N + 2);
+    c.scan_tmp2 = cv.take<char>(scan_tmp_bytes(2 * N + 2));
+  } else {
+    c.nd2 = nullptr;
+    c.newidx = nullptr;
+    c.X2 = nullptr;
+    c.scan_tmp2 = nullptr;
+  }
   c.pcode = cv.take<long long>(N + 1);
   c.pX = cv.take<long long>(N + 1);
   c.Pk = cv.take<int>(N);
@@ -116,19 +127,19 @@ static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S)
   sg.res = cv.take<hbtu_result>(S);
 }
 
-size_t workspace_bytes(long long N, long long S)
+size_t workspace_bytes(long long N, long long S, bool sibling)
 {
   Carver cv(nullptr);
   Ctx c;
   Staging sg;
-  carve(cv, c, sg, N, S);
+  carve(cv, c, sg, N, S, sibling);
   return cv.off + 256;
 }
 
-void carve_workspace(char *base, Ctx &c, Staging &sg, long long N, long long S)
+void carve_workspace(char *base, Ctx &c, Staging &sg, long long N, long long S, bool sibling)
 {
   Carver cv(base);
-  carve(cv, c, sg, N, S);
+  carve(cv, c, sg, N, S, sibling);
 }
 
 // Message of the last failed call made without a handle (fixed buffer: the
@@ -237,6 +248,7 @@ hbtu_status setup_call(hbtu_handle *h, const hbtu_particles *p, long long S, con
   c.id = (long long *)id;
   c.opt_leaf_runs = (int)h->opt_leaf_runs;
   c.opt_schedule = (int)h->opt_schedule;
+  c.opt_layout = (int)h->opt_layout;
   std::vector<SegState> segs;
   std::vector<int> segoff, order(S);
   init_states(h, S, offsets, st, segs, segoff);
@@ -511,6 +523,11 @@ hbtu_status hbtu_set_option(hbtu_handle *h, const char *name, int64_t value)
     h->opt_schedule = value;
     return HBTU_OK;
   }
+  if (n == "walk_layout") {
+    if (value != 0 && value != 1) return fail(h, HBTU_ERR_INVALID_ARGUMENT, "walk_layout: 0 or 1");
+    h->opt_layout = value;
+    return HBTU_OK;
+  }
   return fail(h, HBTU_ERR_INVALID_ARGUMENT, "unknown option " + n);
 }
 
@@ -524,6 +541,10 @@ hbtu_status hbtu_get_option(const hbtu_handle *h, const char *name, int64_t *val
   }
   if (n == "walk_schedule") {
     *value = h->opt_schedule;
+    return HBTU_OK;
+  }
+  if (n == "walk_layout") {
+    *value = h->opt_layout;
     return HBTU_OK;
   }
   return HBTU_ERR_INVALID_ARGUMENT;

@@ -172,6 +172,14 @@ struct Ctx {
   // nodes (2 per tree particle)
   float4 *nd_abs;
   WNode *nd;
+  // the FP32 walk's layout: the same records with each cell's children in
+  // consecutive slots (m.w = first child's slot instead of the upper
+  // threshold); null when the workspace has no room for it
+  WNode *nd2;
+  int *newidx;
+  long long *X2;
+  void *scan_tmp2;
+  int opt_layout;  // 1: the FP32 lane walk uses nd2
   // partition
   long long *pcode, *pX;
   int *Pk, *Qk;
@@ -187,6 +195,17 @@ void launch_bbox_cube(Ctx &c, int max_chunks);
 void launch_tree_build(Ctx &c, const PassPlan &pl);
 // launchers (walk.cu)
 void launch_walk(Ctx &c, const PassPlan &pl);
+void launch_sibling_layout(Ctx &c, const PassPlan &pl);
+// The FP32 lane walk over the sibling-block records (the tree build then makes
+// them): for trees of at least kSiblingMinTree particles in all, where the
+// faster walk pays for the extra pass over the nodes (the small trees of
+// correction passes do not).
+constexpr int kSiblingMinTree = 1 << 17;
+inline bool sibling_walk(const Ctx &c, const PassPlan &pl)
+{
+  return c.P.precision != HBTU_PRECISION_FP64 && c.opt_schedule == 0 && c.opt_layout && c.nd2 &&
+         pl.ntree_total >= kSiblingMinTree;
+}
 void launch_grad_walk(Ctx &c, const PassPlan &pl);
 // per-subhalo sums of a per-particle double array (input positions), deterministic
 void launch_segment_sums(Ctx &c, const double *x, double *out);

@@ -20,8 +20,10 @@ struct Staging {
 
 // Bytes of device workspace for N particles in S subhaloes, and the carving of
 // one allocation (or static array) of that size into the buffers of Ctx.
-size_t workspace_bytes(long long N, long long S);
-void carve_workspace(char *base, Ctx &c, Staging &sg, long long N, long long S);
+// `sibling`: also the buffers of the FP32 walk's sibling-block node layout.
+size_t workspace_bytes(long long N, long long S, bool sibling = true);
+void carve_workspace(char *base, Ctx &c, Staging &sg, long long N, long long S,
+                     bool sibling = true);
 
 // Loop state of subhalo s before its first pass.
 void init_segment(SegState &g, int off, int n, const hbtu_state &st, long long maxsample);

@@ -22,5 +22,6 @@ struct hbtu_handle {
   // tuning options (hbtu_set_option)
   int64_t opt_leaf_runs = 1;
   int64_t opt_schedule = 0;
+  int64_t opt_layout = 1;
   std::vector<cudaEvent_t> events;  // pool: 4 per pass when timing, 2 per call
 };

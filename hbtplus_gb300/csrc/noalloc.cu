@@ -113,7 +113,7 @@ extern "C" hbtu_status hbtu_unbind_noalloc(const hbtu_params *params, const hbtu
     set_global_error("hbtu_unbind_noalloc: invalid parameters");
     return HBTU_ERR_INVALID_ARGUMENT;
   }
-  if (workspace_bytes(HBTU_NOALLOC_MAX_PARTICLES, 1) > kScratchBytes) {
+  if (workspace_bytes(HBTU_NOALLOC_MAX_PARTICLES, 1, false) > kScratchBytes) {
     set_global_error("hbtu_unbind_noalloc: scratch array smaller than its stated capacity");
     return HBTU_ERR_TOO_LARGE;
   }
@@ -123,7 +123,7 @@ extern "C" hbtu_status hbtu_unbind_noalloc(const hbtu_params *params, const hbtu
   try {
     Ctx c;
     Staging sg;
-    carve_workspace(base, c, sg, n, 1);
+    carve_workspace(base, c, sg, n, 1, false);
     PassPlan plan_host;
     c.P = derive_params(*params);
     c.N = (int)n;
@@ -136,6 +136,7 @@ extern "C" hbtu_status hbtu_unbind_noalloc(const hbtu_params *params, const hbtu
     c.id = (long long *)p->id;
     c.opt_leaf_runs = 1;
     c.opt_schedule = 0;
+    c.opt_layout = 0;
     SegState g;
     init_segment(g, 0, (int)n, *st, params->max_sample_size);
     const int segoff[2] = {0, (int)n};

@@ -613,6 +613,112 @@ void launch_tree_build(Ctx &c, const PassPlan &pl)
       HBTU_LAUNCHED();
     }
   }
+  if (sibling_walk(c, pl)) launch_sibling_layout(c, pl);
+}
+
+
+// ---------------------------------------------------------------------------
+// Sibling-block layout for the FP32 lane walk.  The preorder numbering puts a
+// cell's next sibling after the whole subtree of the cell, so a walk that
+// accepts a cell jumps to a far slot.  This copy places the children of every
+// cell in consecutive slots (the children blocks follow the preorder of their
+// cells), keeps each segment's slots, and stores with each cell the slot of
+// its first child; the walk then follows child (open) or skip (accept)
+// pointers: the same nodes in the same order, at other addresses.
+namespace {
+
+// children per node slot, as int64 for the scan (cells only; particles and
+// empty slots keep 0)
+__global__ void __launch_bounds__(kTB) k_sib_count(Ctx c, int ntotal)
+{
+  const int e = blockIdx.x * kTB + threadIdx.x;
+  if (e >= ntotal || !c.iscell[e]) return;
+  const int s = c.sb.hi_a[e];
+  const int idx = c.cidx[e], end = c.cskip[e];
+  int k = 0;
+  if (c.cdepth[e] < c.seg[s].levels) {
+    for (int j = 0; j < 8; j++) {
+      const int sl = c.cslot[8 * e + j];
+      k += (sl > idx && sl < end);
+    }
+  } else {  // a bucket: its particles follow it, one after another
+    k = end - idx - 1;
+  }
+  c.X2[idx] = k;
+}
+
+// the slots of every cell's children: its block starts after the blocks of
+// the cells before it in preorder
+__global__ void __launch_bounds__(kTB) k_sib_assign(Ctx c, int ntotal)
+{
+  const int e = blockIdx.x * kTB + threadIdx.x;
+  if (e >= ntotal || !c.iscell[e]) return;
+  const int s = c.sb.hi_a[e];
+  const int root = 2 * c.tree_base[s];
+  const int idx = c.cidx[e], end = c.cskip[e];
+  const int base = root + 1 + (int)(c.X2[idx] - c.X2[root]);
+  if (idx == root) c.newidx[root] = root;
+  int k = 0;
+  if (c.cdepth[e] < c.seg[s].levels) {
+    for (int j = 0; j < 8; j++) {
+      const int sl = c.cslot[8 * e + j];
+      if (sl > idx && sl < end) c.newidx[sl] = base + k++;
+    }
+  } else {
+    for (int d = idx + 1; d < end; d++) c.newidx[d] = base + k++;
+  }
+}
+
+// a segment of one particle has no cell records: its two nodes keep their slots
+__global__ void k_sib_single(Ctx c)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= c.S) return;
+  const SegState &sg = c.seg[s];
+  if (sg.status != SEG_ACTIVE || c.tree_base[s + 1] - c.tree_base[s] != 1) return;
+  const int root = 2 * c.tree_base[s];
+  c.newidx[root] = root;
+  c.newidx[root + 1] = root + 1;
+}
+
+// every live node slot: its record at its new slot, pointers renumbered
+__global__ void __launch_bounds__(kTB) k_sib_copy(Ctx c, int nslots)
+{
+  const int d = blockIdx.x * kTB + threadIdx.x;
+  if (d >= nslots) return;
+  const int s = upper_bound_i(c.tree_base, c.S + 1, d >> 1) - 1;
+  if (s < 0 || s >= c.S) return;
+  const int root = 2 * c.tree_base[s];
+  const int nn = c.seg[s].nnodes;
+  if (d - root >= nn || c.tree_base[s + 1] == c.tree_base[s]) return;
+  const int nd = c.newidx[d];
+  if (nd < root || nd >= root + nn) return;  // never written: leave the slot alone
+  WNode w = c.nd[d];
+  const int skip = w.m.y;
+  w.m.y = (skip >= root && skip < root + nn) ? c.newidx[skip] : kDone;
+  const bool cell = signbit(w.p.w) != 0;
+  w.m.w = (cell && d + 1 < root + nn) ? c.newidx[d + 1] : kDone;
+  c.nd2[nd] = w;
+}
+
+}  // namespace
+
+void launch_sibling_layout(Ctx &c, const PassPlan &pl)
+{
+  const int n = pl.ntree_total;
+  if (n <= 0 || !c.nd2) return;
+  const int nslots = 2 * n;
+  HBTU_CUDA(cudaMemsetAsync(c.X2, 0, sizeof(long long) * (size_t)(nslots + 1), c.st));
+  HBTU_CUDA(cudaMemsetAsync(c.newidx, 0xff, sizeof(int) * (size_t)nslots, c.st));  // -1
+  k_sib_count<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  HBTU_LAUNCHED();
+  exclusive_scan_i64(c.X2, c.X2, nslots + 1, c.scan_tmp2, c.st);
+  k_sib_assign<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  HBTU_LAUNCHED();
+  k_sib_single<<<(c.S + 127) / 128, 128, 0, c.st>>>(c);
+  HBTU_LAUNCHED();
+  k_sib_copy<<<nblk(nslots), kTB, 0, c.st>>>(c, nslots);
+  HBTU_LAUNCHED();
 }
 
 }  // namespace hbtu

@@ -308,9 +308,20 @@ __device__ __noinline__ bool exact_open(float4 na, float qx, float qy, float qz,
 // per-cell thresholds precomputed from len^2/theta^2 (the reference's double
 // test decides the rare cases in between), every interaction goes straight
 // into a compensated float sum, and the walk ends when the index leaves the
-// tree (skip pointers that leave it are kDone).  The index strictly grows,
-// so the loop ends even on a malformed tree.
-template <int kB>
+// tree (skip pointers that leave it are kDone).
+//   kSib = false: preorder records; the next node is cur + 1 on opening, the
+//     skip pointer otherwise, so the index strictly grows and the loop ends
+//     even on a malformed tree.
+//   kSib = true: the sibling-block records (nd2): a cell's children sit in
+//     consecutive slots, so the sibling an accepted cell hands on to is
+//     usually in the same cache line; the next node is the first-child
+//     pointer (m.w) on opening and the skip pointer otherwise, the upper
+//     threshold is recomputed from the lower one, and the loop also stops
+//     after as many steps as the tree has nodes.  Same nodes, same order,
+//     same sums as the preorder walk.
+constexpr float kBandRatio = 1.0000200002f;  // (1 + 1e-5) / (1 - 1e-5), rounded up
+
+template <int kB, bool kSib>
 __global__ void __launch_bounds__(kB) k_walk_fp32_lean(Ctx c, int total)
 {
   const DevParams &P = c.P;
@@ -318,16 +329,19 @@ __global__ void __launch_bounds__(kB) k_walk_fp32_lean(Ctx c, int total)
   load_target<true>(c, blockIdx.x * kB + threadIdx.x, total, t);
   const float hf = (float)P.h, hinvf = (float)P.h_inv, h2f = hf * hf;
   const double th2d = (double)P.theta2;
+  const WNode *nodes = kSib ? c.nd2 : c.nd;
   float hi = 0.f, comp = 0.f;  // Kahan sum
   int iters = 0, opens = 0;
   int cur = t.nxt;
   const int end = t.end;
+  const int steps = kSib ? max(end - t.nxt, 0) : 0;  // the tree's node count
   while (cur < end) {
     float4 na;
     int4 nm;
-    load_node(c.nd, cur, na, nm);
+    load_node(nodes, cur, na, nm);
     const float r2 = dist2(na, t.q);
-    const float lo = __int_as_float(nm.z), up = __int_as_float(nm.w);
+    const float lo = __int_as_float(nm.z);
+    const float up = kSib ? lo * kBandRatio : __int_as_float(nm.w);
     bool open = r2 < lo;
     if (r2 >= lo && r2 <= up)
       open = exact_open(na, t.q[0], t.q[1], t.q[2], __int_as_float(nm.x & 0x7fffffff), th2d);
@@ -342,11 +356,27 @@ __global__ void __launch_bounds__(kB) k_walk_fp32_lean(Ctx c, int total)
     hi = s;
     iters++;
     opens += open ? 1 : 0;
-    cur = open ? cur + 1 : max(nm.y, cur + 1);
+    if (kSib) {
+      cur = open ? nm.w : nm.y;
+      if (iters >= steps || cur < t.nxt) break;  // malformed pointers: stop
+    } else {
+      cur = open ? cur + 1 : max(nm.y, cur + 1);
+    }
   }
   const double base = (double)__fdiv_rn(t.mself, P.eps);  // cancels the self term
   finish_target(c, t, dadd(dadd(base, (double)hi), -(double)comp));
   count_interactions(c, t.s, iters - opens);
+}
+
+template <bool kSib>
+void launch_lean(Ctx &c, int n)
+{
+  if (n >= 152 * 4 * 512)  // blocks of neighbouring targets share an SM's L1
+    k_walk_fp32_lean<512, kSib><<<(n + 511) / 512, 512, 0, c.st>>>(c, n);
+  else if (n >= 152 * 4 * 256)
+    k_walk_fp32_lean<256, kSib><<<(n + 255) / 256, 256, 0, c.st>>>(c, n);
+  else
+    k_walk_fp32_lean<128, kSib><<<(n + 127) / 128, 128, 0, c.st>>>(c, n);
 }
 
 // FP64: the reference's arithmetic, operation by operation.
@@ -514,12 +544,10 @@ void launch_walk(Ctx &c, const PassPlan &pl)
     k_walk_fp32<true><<<blocks, kWB, 0, c.st>>>(c, n);
   else if (c.opt_schedule == 1)
     k_walk_fp32<false><<<blocks, kWB, 0, c.st>>>(c, n);
-  else if (n >= 152 * 4 * 512)  // blocks of neighbouring targets share an SM's L1
-    k_walk_fp32_lean<512><<<(n + 511) / 512, 512, 0, c.st>>>(c, n);
-  else if (n >= 152 * 4 * 256)
-    k_walk_fp32_lean<256><<<(n + 255) / 256, 256, 0, c.st>>>(c, n);
+  else if (sibling_walk(c, pl))  // the tree build made the sibling-block records
+    launch_lean<true>(c, n);
   else
-    k_walk_fp32_lean<128><<<(n + 127) / 128, 128, 0, c.st>>>(c, n);
+    launch_lean<false>(c, n);
   HBTU_LAUNCHED();
 }
 
