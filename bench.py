@@ -44,7 +44,7 @@ HBM_BYTES_PER_EVALUATION = 44  # read pos, vel, mass (28 B); write E and index (
 FP32_LANES_PER_SM = 128
 # DRAM bytes (read + write) of the first-pass walk launch, from one ncu capture of
 # the same workload (summaries in profiles/); None until captured for this kernel.
-WALK1_DRAM_BYTES = {"batch": 82099200}
+WALK1_DRAM_BYTES = {"batch": 79971584}
 WALK1_PROFILE = {"batch": "walk_lean_pass1_batch2000.md"}
 # The same capture: the walk is limited by the L1 data path, not by DRAM or the FP32 pipe.
 WALK1_LIMITER = {"batch": "L1 data path: l1tex throughput 91% of peak, 22 sectors per warp "
