@@ -47,8 +47,9 @@ FP32_LANES_PER_SM = 128
 WALK1_DRAM_BYTES = {"batch": 79971584}
 WALK1_PROFILE = {"batch": "walk_lean_pass1_batch2000.md"}
 # The same capture: the walk is limited by the L1 data path, not by DRAM or the FP32 pipe.
-WALK1_LIMITER = {"batch": "L1 data path: l1tex throughput 91% of peak, 22 sectors per warp "
-                          "request (one 32-byte node record per lane per step)"}
+WALK1_LIMITER = {"batch": "L1 data path: l1tex throughput 90% of peak at a 97% L1 hit rate, "
+                          "22 sectors per warp request (one 32-byte node record per lane per "
+                          "step; the lanes walk apart)"}
 
 
 def parse():
@@ -498,7 +499,7 @@ def main():
     traffic = WALK1_DRAM_BYTES.get(args.workload) if args.precision == "fp32" else None
     roofline = {
         "kernel": "k_walk_fp32_lean, first pass of the step (Barnes-Hut energy walk, one "
-                  "walk per lane)",
+                  "walk per lane, sibling-block node records)",
         "limiter": WALK1_LIMITER.get(args.workload) if args.precision == "fp32" else None,
         "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
         "frac": achieved / fp32_peak if fp32_peak else None,
