@@ -200,7 +200,7 @@ void launch_sibling_layout(Ctx &c, const PassPlan &pl);
 // them): for trees of at least kSiblingMinTree particles in all, where the
 // faster walk pays for the extra pass over the nodes (the small trees of
 // correction passes do not).
-constexpr int kSiblingMinTree = 1 << 17;
+constexpr int kSiblingMinTree = 1 << 16;
 inline bool sibling_walk(const Ctx &c, const PassPlan &pl)
 {
   return c.P.precision != HBTU_PRECISION_FP64 && c.opt_schedule == 0 && c.opt_layout && c.nd2 &&
