@@ -85,14 +85,11 @@ def merge_subhalos(ub, state: dict, isnap: int, relax: float = 3.0) -> dict:
     def merge_to(s: int, h: int) -> None:  # Subhalo_t::MergeTo
         if nbound[s] <= 1:
             return
-        seen = set(ids[lists[h]].tolist())
-        keep = []
-        for r in lists[s].tolist():
-            i = int(ids[r])
-            if i not in seen:
-                seen.add(i)
-                keep.append(r)
-        lists[h] = np.concatenate([lists[h], np.asarray(keep, np.int64)])
+        cid = ids[lists[s]]
+        first = np.zeros(len(cid), bool)  # first appearance of each Id in the subhalo's list
+        first[np.unique(cid, return_index=True)[1]] = True
+        keep = first & ~np.isin(cid, ids[lists[h]])  # and not held by the sink already
+        lists[h] = np.concatenate([lists[h], lists[s][keep]])
         nbound[h] += nbound[s]
         lists[s] = lists[s][:1]
         nbound[s] = 1
