@@ -154,6 +154,26 @@ void set_global_error(const char *fmt, ...)
   va_end(ap);
 }
 
+hbtu_status grow_workspace(hbtu_handle *h, size_t need)
+{
+  if (need <= h->ws_bytes) return HBTU_OK;
+  if (h->ws) {
+    cudaStreamSynchronize(h->stream);
+    cudaFree(h->ws);
+    h->ws = nullptr;
+    h->ws_bytes = 0;
+  }
+  const size_t bytes = need + need / 4;  // headroom for the next, slightly larger call
+  if (cudaMalloc(&h->ws, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    h->ws = nullptr;
+    h->err = "device workspace of " + std::to_string(bytes) + " bytes could not be allocated";
+    return HBTU_ERR_OUT_OF_MEMORY;
+  }
+  h->ws_bytes = bytes;
+  return HBTU_OK;
+}
+
 namespace {
 
 int max_passes_of(const hbtu_params &p) { return p.max_passes > 0 ? p.max_passes : 10000; }
@@ -167,23 +187,7 @@ hbtu_status fail(hbtu_handle *h, hbtu_status st, const std::string &msg)
 
 hbtu_status ensure_workspace(hbtu_handle *h, long long N, long long S)
 {
-  const size_t need = workspace_bytes(N, S);
-  if (need <= h->ws_bytes) return HBTU_OK;
-  if (h->ws) {
-    cudaStreamSynchronize(h->stream);
-    cudaFree(h->ws);
-    h->ws = nullptr;
-    h->ws_bytes = 0;
-  }
-  size_t bytes = need + need / 4;  // headroom for the next, slightly larger batch
-  if (cudaMalloc(&h->ws, bytes) != cudaSuccess) {
-    cudaGetLastError();
-    h->ws = nullptr;
-    return fail(h, HBTU_ERR_OUT_OF_MEMORY,
-                "device workspace of " + std::to_string(bytes) + " bytes could not be allocated");
-  }
-  h->ws_bytes = bytes;
-  return HBTU_OK;
+  return grow_workspace(h, workspace_bytes(N, S));
 }
 
 void init_states(const hbtu_handle *h, long long S, const int64_t *offsets, const hbtu_state *st,

@@ -25,3 +25,9 @@ struct hbtu_handle {
   int64_t opt_layout = 1;
   std::vector<cudaEvent_t> events;  // pool: 4 per pass when timing, 2 per call
 };
+
+namespace hbtu {
+// The handle's device workspace grown to at least `need` bytes (its contents
+// are not kept); the calls on one handle share it.
+hbtu_status grow_workspace(hbtu_handle *h, size_t need);
+}  // namespace hbtu

@@ -177,23 +177,8 @@ extern "C" hbtu_status hbtu_merge_detect(hbtu_handle *h, const hbtu_particles *p
   const size_t total = a256(sizeof(MergeSeg) * nsub) + a256(sizeof(hbtu_core) * nsub) +
                        2 * a256(12 * nsub) + a256(8 * nsub) + 2 * a256(4 * nsub) + 256 +
                        (hostmem ? 2 * a256(12 * N) + a256(4 * N) : 0);
-  if (total > h->ws_bytes) {
-    if (h->ws) {
-      cudaStreamSynchronize(st);
-      cudaFree(h->ws);
-      h->ws = nullptr;
-      h->ws_bytes = 0;
-    }
-    const size_t bytes = total + total / 4;
-    if (cudaMalloc(&h->ws, bytes) != cudaSuccess) {
-      cudaGetLastError();
-      h->ws = nullptr;
-      h->err = "merge detect: device workspace of " + std::to_string(bytes) +
-               " bytes could not be allocated";
-      return HBTU_ERR_OUT_OF_MEMORY;
-    }
-    h->ws_bytes = bytes;
-  }
+  const hbtu_status ws = grow_workspace(h, total);
+  if (ws != HBTU_OK) return ws;
   char *mem = h->ws;
   size_t o = 0;
   auto take = [&](size_t bytes) {

@@ -442,23 +442,8 @@ extern "C" hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_partic
         a256(scan_tmp_bytes(T + 1)) + 256;
     // the handle's workspace (the unbinding's buffers are larger, so it is
     // normally in place already)
-    if (total > h->ws_bytes) {
-      if (h->ws) {
-        cudaStreamSynchronize(st);
-        cudaFree(h->ws);
-        h->ws = nullptr;
-        h->ws_bytes = 0;
-      }
-      const size_t bytes = total + total / 4;
-      if (cudaMalloc(&h->ws, bytes) != cudaSuccess) {
-        cudaGetLastError();
-        h->ws = nullptr;
-        h->err = "subhalo properties: device workspace of " + std::to_string(bytes) +
-                 " bytes could not be allocated";
-        return HBTU_ERR_OUT_OF_MEMORY;
-      }
-      h->ws_bytes = bytes;
-    }
+    const hbtu_status ws = grow_workspace(h, total);
+    if (ws != HBTU_OK) return ws;
     mem = h->ws;
     size_t o = 0;
     auto take = [&](size_t bytes) {
