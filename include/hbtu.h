@@ -206,7 +206,11 @@ hbtu_status hbtu_reset_stats(hbtu_handle *h);
  *                     lane walks its own target; 1 a warp visits the smallest
  *                     node index any of its targets waits at (broadcast loads).
  *   "walk_leaf_runs"  1 (default) or 0: with walk_schedule 1, stream the
- *                     particles of a cell whose children are all particles. */
+ *                     particles of a cell whose children are all particles.
+ *   "walk_layout"     1 (default) or 0: with walk_schedule 0, passes whose
+ *                     trees hold at least 2^16 particles in all walk a copy
+ *                     of the node records with every cell's children in
+ *                     consecutive slots (0: the preorder records). */
 hbtu_status hbtu_set_option(hbtu_handle *h, const char *name, int64_t value);
 hbtu_status hbtu_get_option(const hbtu_handle *h, const char *name, int64_t *value);
 
