@@ -595,7 +595,7 @@ def main():
     accuracy = None
     if args.workload == "host2e7":
         args.no_cpu = True  # the CPU path needs several minutes per unbinding of 2.7e7 particles
-    if not args.no_cpu:
+    if not args.no_cpu and ws == 1:  # the CPU baseline: rank 0 at N = 1 only
         threads = cpu_threads()
         t_cpu, kind, cres = cpu_reference_time(params, batch, threads)
         cpu = {"value": nsub / t_cpu, "unit": UNIT, "cores": threads, "kind": kind,
@@ -630,7 +630,8 @@ def main():
                               "loop": st["loop_ms"] / args.steps,
                               "passes": st["passes"] / args.steps},
     }
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
