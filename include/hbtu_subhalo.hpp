@@ -5,6 +5,9 @@
 //   hbtu::UnbindBatchGPU(handle, params, subhaloes, ids, snapshot)
 //       replaces  the per-subhalo Unbind loops of SubhaloSnapshot_t::RefineParticles
 //                 (src/subhalo_unbind.cpp:471-513), one call per nesting level
+//   hbtu::PropertiesGPU(handle, subhaloes, ids, snapshot)
+//       replaces  the CalculateProfileProperties + CalculateShape loop at the end
+//                 of SubhaloSnapshot_t::UpdateTracks (src/subhalo_tracking.cpp:901-906)
 //
 // Templated on the caller's Subhalo_t / Snapshot_t, using the member names of
 // src/subhalo.h:24-146 and src/snapshot.h:51-111, so it compiles against the
@@ -161,6 +164,64 @@ hbtu_status UnbindBatchGPU(hbtu_handle *h, const hbtu_params &params, SubhaloLis
     detail::apply(subhaloes[ids[k]], epoch, r[k], order.data() + off[k], energy.data() + off[k],
                   (std::vector<float> *)nullptr);
   return rc;
+}
+
+// Subhalo_t::CalculateProfileProperties and ::CalculateShape
+// (src/subhalo.cpp:242-398) of subhaloes[ids[k]] for every k, in one device
+// call, on their bound particles (Particles[0 .. Nbound), most-bound first, as
+// Unbind leaves them).  A subhalo with Nbound <= 1 is left as it is, as in the
+// reference.
+template <class SubhaloListT, class SnapshotT>
+hbtu_status PropertiesGPU(hbtu_handle *h, SubhaloListT &subhaloes, const std::vector<int64_t> &ids,
+                          const SnapshotT &epoch)
+{
+  SubhaloArrays a;
+  std::vector<int64_t> off(1, 0), order;
+  std::vector<hbtu_result> r;
+  std::vector<float> last_max;
+  std::vector<int32_t> last_snap;
+  for (int64_t k : ids) {
+    auto &s = subhaloes[k];
+    const int64_t n = (int64_t)s.Particles.size();
+    detail::gather(s.Particles, a);
+    for (int64_t i = 0; i < n; i++) order.push_back(i);  // Particles are in bound order already
+    off.push_back(off.back() + n);
+    hbtu_result q{};
+    q.nbound = (int64_t)s.Nbound;
+    q.mbound = (float)s.Mbound;
+    for (int j = 0; j < 3; j++) q.mostbound_pos[j] = (float)s.ComovingMostBoundPosition[j];
+    r.push_back(q);
+    last_max.push_back((float)s.LastMaxVmaxPhysical);
+    last_snap.push_back((int32_t)s.SnapshotIndexOfLastMaxVmax);
+  }
+  const int64_t nsub = (int64_t)ids.size();
+  if (nsub == 0) return HBTU_OK;
+  hbtu_particles p{a.id.data(), a.pos.data(), a.vel.data(), a.mass.data(), a.type.data(),
+                   HBTU_HOST, 0};
+  if (order.empty()) order.push_back(0);
+  std::vector<hbtu_props> out(nsub);
+  const hbtu_status rc =
+      hbtu_subhalo_properties(h, &p, nsub, off.data(), order.data(), r.data(), last_max.data(),
+                              last_snap.data(), (int32_t)epoch.GetSnapshotIndex(), out.data());
+  if (rc != HBTU_OK) return rc;
+  for (int64_t k = 0; k < nsub; k++) {
+    auto &s = subhaloes[ids[k]];
+    if (s.Nbound <= 1) continue;  // subhalo.cpp:264-282, :339-351
+    const hbtu_props &q = out[k];
+    s.RmaxComoving = q.rmax_comoving;
+    s.VmaxPhysical = q.vmax_physical;
+    s.LastMaxVmaxPhysical = q.last_max_vmax_physical;
+    s.SnapshotIndexOfLastMaxVmax = q.snapshot_of_last_max_vmax;
+    s.R2SigmaComoving = q.r2sigma_comoving;
+    s.RHalfComoving = q.rhalf_comoving;
+    s.BoundR200CritComoving = q.r200crit_comoving;
+    s.BoundM200Crit = q.m200crit;
+    for (int t = 0; t < 6; t++) {
+      s.InertialTensor[t] = q.inertial_tensor[t];
+      s.InertialTensorWeighted[t] = q.inertial_tensor_weighted[t];
+    }
+  }
+  return HBTU_OK;
 }
 
 }  // namespace hbtu

@@ -32,6 +32,10 @@ struct Subhalo_t {
   HBTxyz ComovingAveragePosition, PhysicalAverageVelocity, ComovingMostBoundPosition,
       PhysicalMostBoundVelocity;
   long SinkTrackId = -1;
+  float RmaxComoving = 0, VmaxPhysical = 0, LastMaxVmaxPhysical = 0;
+  int SnapshotIndexOfLastMaxVmax = -1;
+  float R2SigmaComoving = 0, RHalfComoving = 0, BoundR200CritComoving = 0, BoundM200Crit = 0;
+  float InertialTensor[6] = {0}, InertialTensorWeighted[6] = {0};
   std::vector<Particle_t> Particles;
   bool IsTrapped() { return SinkTrackId != -1; }
   bool IsAlive() { return SnapshotIndexOfDeath == -1; }
@@ -81,4 +85,47 @@ extern "C" int shim_unbind(hbtu_handle *h, const hbtu_params *par, int64_t n, co
   for (int t = 0; t < 6; t++) out->nbound_type[t] = s.NboundType[t];
   *death = s.SnapshotIndexOfDeath;
   return HBTU_OK;
+}
+
+// One subhalo as Unbind leaves it (particles bound first), through
+// hbtu::PropertiesGPU at snapshot 7; the property members come back in `out`
+// (the layout of hbtu_props).
+extern "C" int shim_properties(hbtu_handle *h, int64_t n, const int64_t *id, const float *pos,
+                               const float *mass, int64_t nbound, float mbound,
+                               const float *mostbound_pos, float last_max_vmax,
+                               int32_t last_snap, hbtu_props *out)
+{
+  std::vector<mock::Subhalo_t> subs(1);
+  mock::Subhalo_t &s = subs[0];
+  s.Particles.resize(n);
+  for (int64_t i = 0; i < n; i++) {
+    s.Particles[i].Id = id[i];
+    for (int j = 0; j < 3; j++) {
+      s.Particles[i].ComovingPosition[j] = pos[3 * i + j];
+      s.Particles[i].PhysicalVelocity[j] = 0.f;
+    }
+    s.Particles[i].Mass = mass[i];
+    s.Particles[i].Type = 1;
+  }
+  s.Nbound = nbound;
+  s.Mbound = mbound;
+  for (int j = 0; j < 3; j++) s.ComovingMostBoundPosition[j] = mostbound_pos[j];
+  s.LastMaxVmaxPhysical = last_max_vmax;
+  s.SnapshotIndexOfLastMaxVmax = last_snap;
+  mock::Snapshot_t epoch;
+  const hbtu_status rc = hbtu::PropertiesGPU(h, subs, {0}, epoch);
+  if (rc != HBTU_OK) return rc;
+  out->rmax_comoving = s.RmaxComoving;
+  out->vmax_physical = s.VmaxPhysical;
+  out->last_max_vmax_physical = s.LastMaxVmaxPhysical;
+  out->snapshot_of_last_max_vmax = s.SnapshotIndexOfLastMaxVmax;
+  out->r2sigma_comoving = s.R2SigmaComoving;
+  out->rhalf_comoving = s.RHalfComoving;
+  out->r200crit_comoving = s.BoundR200CritComoving;
+  out->m200crit = s.BoundM200Crit;
+  for (int t = 0; t < 6; t++) {
+    out->inertial_tensor[t] = s.InertialTensor[t];
+    out->inertial_tensor_weighted[t] = s.InertialTensorWeighted[t];
+  }
+  return 0;
 }

@@ -4,7 +4,9 @@ CPU: the shim compiles against stand-ins with the reference's member names
 (tests/shim/shim_lib.cpp) and, where the reference sources are present,
 against the reference's own headers.  GPU: the compiled harness unbinds golden
 subhaloes through hbtu::UnbindGPU and leaves them as the reference's Unbind
-does (FP64 mode: bit-exact Nbound, Mbound, order and Energies)."""
+does (FP64 mode: bit-exact Nbound, Mbound, order and Energies), and computes
+their profile and shape through hbtu::PropertiesGPU as the reference's
+CalculateProfileProperties and CalculateShape do (tests/golden/props_10.npz)."""
 import ctypes as C
 import os
 import subprocess
@@ -40,7 +42,8 @@ def test_shim_compiles_against_reference_types(tmp_path):
     src.write_text('#include "subhalo.h"\n#include "hbtu_subhalo.hpp"\n'
                    "void f(hbtu_handle *h, const hbtu_params &p, Subhalo_t &s, const Snapshot_t &e)"
                    "{ std::vector<float> E; hbtu::UnbindGPU(h, p, s, e, &E); "
-                   "std::vector<Subhalo_t> v(1); hbtu::UnbindBatchGPU(h, p, v, {0}, e); }\n")
+                   "std::vector<Subhalo_t> v(1); hbtu::UnbindBatchGPU(h, p, v, {0}, e); "
+                   "hbtu::PropertiesGPU(h, v, {0}, e); }\n")
     subprocess.run(["g++", "-std=c++11", "-fsyntax-only", "-DHBT_INT8", "-w",
                     "-I", os.path.join(ROOT, "oracle", "ref", "stubs"), "-I", REF_SRC,
                     "-I", os.path.join(ROOT, "include"), str(src)], check=True)
@@ -80,3 +83,42 @@ def test_shim_unbind_matches_reference(case):
         np.testing.assert_array_equal(out_e[:nb], ref["energy"][:nb])
         assert set(out_id[:nb].tolist()) == set(ref_ids[:nb].tolist())
         assert death.value == -1
+
+
+@pytest.mark.gpu
+def test_shim_properties_match_reference():
+    """The profile and shape of the reference's unbound subhaloes (props_10:
+    the reference's order, Nbound, Mbound and most-bound position), computed
+    through hbtu::PropertiesGPU with the member names of Subhalo_t."""
+    from hbtplus_gb300 import _lib
+    from hbtplus_gb300.unbind import Unbinder
+    from test_props import SCALARS, TENSORS, compare, fixture_props, load
+    so = C.CDLL(build_shim())
+    par, b, ref, props, snap = load("props_10")  # the fixture's epoch is snapshot 1
+    with Unbinder(par) as ub:
+        for s in range(len(b["offsets"]) - 1):
+            o0, o1 = int(b["offsets"][s]), int(b["offsets"][s + 1])
+            idx = o0 + ref["order"][o0:o1]  # the particles as Unbind leaves them
+            pos = np.ascontiguousarray(b["pos"][idx], np.float32)
+            mass = np.ascontiguousarray(b["mass"][idx], np.float32)
+            ids = np.ascontiguousarray(b["id"][idx], np.int64)
+            mbp = np.ascontiguousarray(ref["mostbound_pos"][s], np.float32)
+            out = _lib.hbtu_props()
+            rc = so.shim_properties(ub.handle, C.c_int64(o1 - o0), C.c_void_p(ids.ctypes.data),
+                                    C.c_void_p(pos.ctypes.data), C.c_void_p(mass.ctypes.data),
+                                    C.c_int64(int(ref["nbound"][s])),
+                                    C.c_float(float(ref["mbound"][s])),
+                                    C.c_void_p(mbp.ctypes.data),
+                                    C.c_float(float(b["last_max_vmax"][s])),
+                                    C.c_int32(int(b["last_snap"][s])), C.byref(out))
+            assert rc == 0
+            got = {k: getattr(out, k) for k in SCALARS + TENSORS}
+            got = {k: (np.array(list(v), np.float32) if hasattr(v, "__len__") else v)
+                   for k, v in got.items()}
+            want = fixture_props(props, s)
+            if int(ref["nbound"][s]) > 1:
+                # the harness's epoch is snapshot 7 and the fixture's 1: the index of the
+                # last maximum follows the epoch, everything else the particles
+                if want["snapshot_of_last_max_vmax"] == snap:
+                    want["snapshot_of_last_max_vmax"] = 7
+                compare(got, want, ("shim", s))
