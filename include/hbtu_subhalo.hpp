@@ -8,6 +8,9 @@
 //   hbtu::PropertiesGPU(handle, subhaloes, ids, snapshot)
 //       replaces  the CalculateProfileProperties + CalculateShape loop at the end
 //                 of SubhaloSnapshot_t::UpdateTracks (src/subhalo_tracking.cpp:901-906)
+//   hbtu::DetectTrapsGPU(handle, subhaloes, snapshot, merged)
+//       replaces  FillHelpers + DetectTraps of SubhaloSnapshot_t::MergeSubhalos
+//                 (src/subhalo_merge.cpp:30-180, :193-199)
 //
 // Templated on the caller's Subhalo_t / Snapshot_t, using the member names of
 // src/subhalo.h:24-146 and src/snapshot.h:51-111, so it compiles against the
@@ -220,6 +223,67 @@ hbtu_status PropertiesGPU(hbtu_handle *h, SubhaloListT &subhaloes, const std::ve
       s.InertialTensor[t] = q.inertial_tensor[t];
       s.InertialTensorWeighted[t] = q.inertial_tensor_weighted[t];
     }
+  }
+  return HBTU_OK;
+}
+
+// FillHelpers + DetectTraps of SubhaloSnapshot_t::MergeSubhalos
+// (src/subhalo_merge.cpp:30-180) for every subhalo, on the GPU.  Call it where
+// MergeSubhalos fills its helpers, with the head nests glued (GlueHeadNests):
+// the host of a subhalo is the subhalo whose NestedSubhalos lists it (the last
+// one in index order).  Writes SinkTrackId and SnapshotIndexOfSink of the
+// subhaloes trapped now and returns, per subhalo, the IsMerged flag of its
+// helper (it swallows a subhalo with Nbound > 1).  The core of a subhalo reads
+// its first min(Nbound, 20) particles, so only those are sent.
+template <class SubhaloListT, class SnapshotT>
+hbtu_status DetectTrapsGPU(hbtu_handle *h, SubhaloListT &subhaloes, const SnapshotT &epoch,
+                           std::vector<char> &merged)
+{
+  const int64_t nsub = (int64_t)subhaloes.size();
+  merged.assign(nsub, 0);
+  if (nsub == 0) return HBTU_OK;
+  SubhaloArrays a;
+  std::vector<int64_t> off(1, 0), nbound(nsub), host(nsub, -1), sink(nsub);
+  std::vector<float> mbp(3 * nsub), mbv(3 * nsub);
+  std::vector<int32_t> sink_snap(nsub), flag(nsub);
+  for (int64_t i = 0; i < nsub; i++) {
+    auto &s = subhaloes[i];
+    for (auto c : s.NestedSubhalos) host[(int64_t)c] = i;  // FillHostTrackIds (:162-171)
+    const int64_t nb = (int64_t)s.Nbound;
+    const int64_t ncore = std::min<int64_t>({nb > 0 ? nb : 0, (int64_t)s.Particles.size(), 20});
+    typename std::decay<decltype(s.Particles)>::type core(s.Particles.begin(),
+                                                          s.Particles.begin() + ncore);
+    detail::gather(core, a);
+    off.push_back(off.back() + ncore);
+    nbound[i] = nb;
+    sink[i] = (int64_t)s.SinkTrackId;
+    sink_snap[i] = (int32_t)s.SnapshotIndexOfSink;
+    for (int j = 0; j < 3; j++) {
+      mbp[3 * i + j] = (float)s.ComovingMostBoundPosition[j];
+      mbv[3 * i + j] = (float)s.PhysicalMostBoundVelocity[j];
+    }
+  }
+  if (a.mass.empty()) {  // no particles at all: keep the pointers valid
+    a.id.push_back(0);
+    a.mass.push_back(0.f);
+    a.type.push_back(1);
+    for (int j = 0; j < 3; j++) {
+      a.pos.push_back(0.f);
+      a.vel.push_back(0.f);
+    }
+  }
+  hbtu_particles p{a.id.data(), a.pos.data(), a.vel.data(), a.mass.data(), a.type.data(),
+                   HBTU_HOST, 0};
+  const hbtu_status rc = hbtu_merge_detect(h, &p, nsub, off.data(), nbound.data(), host.data(),
+                                           mbp.data(), mbv.data(),
+                                           (int32_t)epoch.GetSnapshotIndex(), sink.data(),
+                                           sink_snap.data(), flag.data(), nullptr);
+  if (rc != HBTU_OK) return rc;
+  for (int64_t i = 0; i < nsub; i++) {
+    auto &s = subhaloes[i];
+    s.SinkTrackId = sink[i];
+    s.SnapshotIndexOfSink = sink_snap[i];
+    merged[i] = flag[i] != 0;
   }
   return HBTU_OK;
 }

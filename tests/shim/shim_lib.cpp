@@ -37,6 +37,7 @@ struct Subhalo_t {
   float R2SigmaComoving = 0, RHalfComoving = 0, BoundR200CritComoving = 0, BoundM200Crit = 0;
   float InertialTensor[6] = {0}, InertialTensorWeighted[6] = {0};
   std::vector<Particle_t> Particles;
+  std::vector<long> NestedSubhalos;
   bool IsTrapped() { return SinkTrackId != -1; }
   bool IsAlive() { return SnapshotIndexOfDeath == -1; }
 };
@@ -126,6 +127,51 @@ extern "C" int shim_properties(hbtu_handle *h, int64_t n, const int64_t *id, con
   for (int t = 0; t < 6; t++) {
     out->inertial_tensor[t] = s.InertialTensor[t];
     out->inertial_tensor_weighted[t] = s.InertialTensorWeighted[t];
+  }
+  return 0;
+}
+
+// Subhaloes as MergeSubhalos finds them (lists bound first, nests glued):
+// hbtu::DetectTrapsGPU at snapshot 7, then SinkTrackId, SnapshotIndexOfSink
+// and the IsMerged flags back.
+extern "C" int shim_detect_traps(hbtu_handle *h, int64_t nsub, const int64_t *list_off,
+                                 const int64_t *id, const float *pos, const float *vel,
+                                 const float *mass, const int64_t *nbound, const float *mb_pos,
+                                 const float *mb_vel, const int64_t *nest_off,
+                                 const int64_t *nest_idx, const int64_t *sink_in,
+                                 int64_t *sink_out, int32_t *sink_snap_out, int32_t *merged_out)
+{
+  std::vector<mock::Subhalo_t> subs(nsub);
+  for (int64_t s = 0; s < nsub; s++) {
+    mock::Subhalo_t &sub = subs[s];
+    for (int64_t i = list_off[s]; i < list_off[s + 1]; i++) {
+      mock::Particle_t q;
+      q.Id = id[i];
+      for (int j = 0; j < 3; j++) {
+        q.ComovingPosition[j] = pos[3 * i + j];
+        q.PhysicalVelocity[j] = vel[3 * i + j];
+      }
+      q.Mass = mass[i];
+      q.Type = 1;
+      sub.Particles.push_back(q);
+    }
+    sub.Nbound = nbound[s];
+    for (int j = 0; j < 3; j++) {
+      sub.ComovingMostBoundPosition[j] = mb_pos[3 * s + j];
+      sub.PhysicalMostBoundVelocity[j] = mb_vel[3 * s + j];
+    }
+    for (int64_t k = nest_off[s]; k < nest_off[s + 1]; k++) sub.NestedSubhalos.push_back(nest_idx[k]);
+    sub.SinkTrackId = sink_in[s];
+    sub.SnapshotIndexOfSink = -1;
+  }
+  mock::Snapshot_t epoch;
+  std::vector<char> merged;
+  const hbtu_status rc = hbtu::DetectTrapsGPU(h, subs, epoch, merged);
+  if (rc != HBTU_OK) return rc;
+  for (int64_t s = 0; s < nsub; s++) {
+    sink_out[s] = subs[s].SinkTrackId;
+    sink_snap_out[s] = subs[s].SnapshotIndexOfSink;
+    merged_out[s] = merged[s];
   }
   return 0;
 }

@@ -6,7 +6,9 @@ against the reference's own headers.  GPU: the compiled harness unbinds golden
 subhaloes through hbtu::UnbindGPU and leaves them as the reference's Unbind
 does (FP64 mode: bit-exact Nbound, Mbound, order and Energies), and computes
 their profile and shape through hbtu::PropertiesGPU as the reference's
-CalculateProfileProperties and CalculateShape do (tests/golden/props_10.npz)."""
+CalculateProfileProperties and CalculateShape do (tests/golden/props_10.npz),
+and finds the reference's sinks through hbtu::DetectTrapsGPU
+(tests/golden/merge_10.npz)."""
 import ctypes as C
 import os
 import subprocess
@@ -43,7 +45,8 @@ def test_shim_compiles_against_reference_types(tmp_path):
                    "void f(hbtu_handle *h, const hbtu_params &p, Subhalo_t &s, const Snapshot_t &e)"
                    "{ std::vector<float> E; hbtu::UnbindGPU(h, p, s, e, &E); "
                    "std::vector<Subhalo_t> v(1); hbtu::UnbindBatchGPU(h, p, v, {0}, e); "
-                   "hbtu::PropertiesGPU(h, v, {0}, e); }\n")
+                   "hbtu::PropertiesGPU(h, v, {0}, e); std::vector<char> m; "
+                   "hbtu::DetectTrapsGPU(h, v, e, m); }\n")
     subprocess.run(["g++", "-std=c++11", "-fsyntax-only", "-DHBT_INT8", "-w",
                     "-I", os.path.join(ROOT, "oracle", "ref", "stubs"), "-I", REF_SRC,
                     "-I", os.path.join(ROOT, "include"), str(src)], check=True)
@@ -122,3 +125,37 @@ def test_shim_properties_match_reference():
                 if want["snapshot_of_last_max_vmax"] == snap:
                     want["snapshot_of_last_max_vmax"] = 7
                 compare(got, want, ("shim", s))
+
+
+@pytest.mark.gpu
+def test_shim_detect_traps_match_reference():
+    """hbtu::DetectTrapsGPU on the subhaloes of merge_10 (nests glued as
+    MergeSubhalos glues them) gives the reference's sinks and merged hosts."""
+    from hbtplus_gb300.merge import glued_nests
+    from hbtplus_gb300.unbind import Unbinder
+    from test_merge import load
+    so = C.CDLL(build_shim())
+    par, st, ref, isnap, relax = load()
+    nests, _ = glued_nests(st)
+    nest_off = np.concatenate([[0], np.cumsum([len(x) for x in nests])]).astype(np.int64)
+    nest_idx = np.array([c for x in nests for c in x], np.int64)
+    nsub = len(st["list_off"]) - 1
+    a = {k: np.ascontiguousarray(st[k]) for k in ("list_off", "id", "pos", "vel", "mass",
+                                                   "nbound", "mostbound_pos", "mostbound_vel",
+                                                   "sink")}
+    sink = np.zeros(nsub, np.int64)
+    snap = np.zeros(nsub, np.int32)
+    merged = np.zeros(nsub, np.int32)
+    ptr = lambda x: C.c_void_p(x.ctypes.data)  # noqa: E731
+    with Unbinder(par) as ub:
+        rc = so.shim_detect_traps(ub.handle, C.c_int64(nsub), ptr(a["list_off"]), ptr(a["id"]),
+                                  ptr(a["pos"]), ptr(a["vel"]), ptr(a["mass"]), ptr(a["nbound"]),
+                                  ptr(a["mostbound_pos"]), ptr(a["mostbound_vel"]),
+                                  ptr(nest_off), ptr(nest_idx), ptr(a["sink"]), ptr(sink),
+                                  ptr(snap), ptr(merged))
+    assert rc == 0
+    assert list(sink) == list(ref["sink"])
+    newly = ref["sink_snap"] == isnap  # trapped at this snapshot (the harness's epoch is 7)
+    assert list(np.nonzero(snap == 7)[0]) == list(np.nonzero(newly)[0])
+    want = {int(ref["sink"][s]) for s in np.nonzero(newly)[0] if st["nbound"][s] > 1}
+    assert set(np.nonzero(merged)[0].tolist()) == want
