@@ -27,7 +27,7 @@ namespace hbtu {
 namespace {
 
 constexpr int kTB = 256;
-constexpr int kLevelSyncMin = 1 << 16;  // tree particles from which moments go level by level
+constexpr int kLevelSyncMin = 1 << 18;  // tree particles from which moments go level by level
 
 __global__ void __launch_bounds__(kTB) k_bbox_chunks(Ctx c)
 {
