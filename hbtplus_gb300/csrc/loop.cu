@@ -27,17 +27,62 @@ constexpr int kSums = 24;  // doubles per reduction chunk
 inline unsigned nblk(long long n, int b = kLB) { return (unsigned)((n + b - 1) / b); }
 
 // ---------------------------------------------------------------- helpers
-template <int K>
-__device__ void block_sum(double (&v)[K], double *out)
+// One step of a warp reduce-scatter of N doubles: the lanes of each pair
+// (lane, lane ^ o) add the same two values as an xor butterfly would, but
+// each keeps only half of them (the lane with bit o set keeps the upper
+// half, indices h .. N-1 with h = ceil(N/2), padded by one zero when N is
+// odd).  Five steps (o = 16 .. 1) leave each sum in one lane, bit-identical
+// to the butterfly's result (same pairs, same order of association).
+template <int N>
+__device__ __forceinline__ void rs_step(const double (&cur)[N], double (&nxt)[(N + 1) / 2], int o,
+                                        bool upper)
 {
+  constexpr int h = (N + 1) / 2;
+#pragma unroll
+  for (int j = 0; j < h; j++) {
+    const double lo = cur[j], hi = (j + h < N) ? cur[j + h] : 0.;
+    const double recv = __shfl_xor_sync(0xffffffffu, upper ? lo : hi, o);
+    nxt[j] = (upper ? hi : lo) + recv;
+  }
+}
+
+// Sums of K values over a block of kLB threads into out[0 .. K).  The
+// chunk's elements p = threadIdx.x + j*kLB (0 <= p < nvalid) are spread over
+// the warps in order, so a warp with 32*w >= nvalid holds only zeros and
+// writes them without reducing (small subhaloes leave most warps empty).
+template <int K>
+__device__ void block_sum(double (&v)[K], double *out, int nvalid)
+{
+  static_assert(K >= 1 && K <= 32, "one sum per lane at most");
   __shared__ double sh[K][kLB / 32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (32 * w < nvalid) {
+    constexpr int n1 = (K + 1) / 2, n2 = (n1 + 1) / 2, n3 = (n2 + 1) / 2, n4 = (n3 + 1) / 2,
+                  n5 = (n4 + 1) / 2;
+    double a1[n1], a2[n2], a3[n3], a4[n4], a5[n5];
+    rs_step<K>(v, a1, 16, lane & 16);
+    rs_step<n1>(a1, a2, 8, lane & 8);
+    rs_step<n2>(a2, a3, 4, lane & 4);
+    rs_step<n3>(a3, a4, 2, lane & 2);
+    rs_step<n4>(a4, a5, 1, lane & 1);
+    // the index of the sum this lane holds: the split follows the padded
+    // sizes N; n counts the lane's real (unpadded) values
+    int base = 0, n = K, N = K;
 #pragma unroll
-  for (int k = 0; k < K; k++)
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-  const int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0)
-#pragma unroll
-    for (int k = 0; k < K; k++) sh[k][w] = v[k];
+    for (int o = 16; o > 0; o >>= 1) {
+      const int h = (N + 1) / 2;
+      if (lane & o) {
+        base += h;
+        n = max(0, n - h);
+      } else {
+        n = min(n, h);
+      }
+      N = h;
+    }
+    if (n >= 1) sh[base][w] = a5[0];
+  } else if (lane < K) {
+    sh[lane][w] = 0.;
+  }
   __syncthreads();
   if (threadIdx.x < K) {
     double t = 0.;
@@ -479,7 +524,7 @@ __global__ void __launch_bounds__(kLB) k_avg_chunks(Ctx c)
       v[6] += f2d(fmul(a.z, m));
     }
   }
-  block_sum<7>(v, c.chunk_sums + (size_t)b * kSums);
+  block_sum<7>(v, c.chunk_sums + (size_t)b * kSums, hi - lo);
 }
 
 // ---------------------------------------------------------------- control
@@ -693,6 +738,7 @@ __global__ void __launch_bounds__(kLB) k_kin_chunks(Ctx c)
   const int lo = ci * kChunk, hi = min(lo + kChunk, nb);
   double v[18];
   for (int k = 0; k < 18; k++) v[k] = 0.;
+  int cnt[6] = {0, 0, 0, 0, 0, 0};
   const double Pa = (double)P.a, PHz = (double)P.Hz;
   for (int p = lo + threadIdx.x; p < hi; p += kLB) {
     const int pid = c.epid[sg.off + p];
@@ -715,14 +761,20 @@ __global__ void __launch_bounds__(kLB) k_kin_chunks(Ctx c)
     v[5] += md;
     const int t = c.type ? c.type[pid] : 1;
     const bool skip = (nb <= 100 && c.id[pid] == -1) || t < 0 || t > 5;
-#pragma unroll
-    for (int q = 0; q < 6; q++)
-      if (!skip && q == t) {
-        v[6 + q] += 1.0;
-        v[12 + q] += md;
+    if (!skip) {
+      switch (t) {  // one double add per particle (the type is nearly always warp-uniform)
+        case 0: cnt[0]++; v[12] += md; break;
+        case 1: cnt[1]++; v[13] += md; break;
+        case 2: cnt[2]++; v[14] += md; break;
+        case 3: cnt[3]++; v[15] += md; break;
+        case 4: cnt[4]++; v[16] += md; break;
+        default: cnt[5]++; v[17] += md; break;
       }
+    }
   }
-  block_sum<18>(v, c.chunk_sums + (size_t)b * kSums);
+#pragma unroll
+  for (int q = 0; q < 6; q++) v[6 + q] = (double)cnt[q];  // exact: counts < 2^53
+  block_sum<18>(v, c.chunk_sums + (size_t)b * kSums, hi - lo);
 }
 
 __global__ void k_final_seg(Ctx c, hbtu_result *res)
@@ -839,7 +891,7 @@ __global__ void __launch_bounds__(kLB) k_segsum_chunks(Ctx c, const double *x)
   const int lo = (b - c.bchunk_base[s]) * kChunk, hi = min(lo + kChunk, sg.n);
   double v[1] = {0.};
   for (int p = lo + threadIdx.x; p < hi; p += kLB) v[0] += x[sg.off + p];
-  block_sum<1>(v, c.chunk_sums + (size_t)b * kSums);
+  block_sum<1>(v, c.chunk_sums + (size_t)b * kSums, hi - lo);
 }
 
 __global__ void k_segsum_combine(Ctx c, double *out)
