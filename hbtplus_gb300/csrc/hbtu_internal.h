@@ -116,6 +116,43 @@ struct CudaError {
   CudaError(cudaError_t e, const char *expr, const char *file, int line);
 };
 
+// Programmatic dependent launch.  The kernels of the unbinding path are
+// launched with programmatic stream serialisation (launch_k), so that a
+// kernel's launch is processed while its predecessor in the stream still
+// runs.  Every such kernel opens with HBTU_KERNEL_PROLOGUE: griddepcontrol.wait
+// returns once all prerequisite grids have completed and their memory is
+// visible, and only then does the kernel let its own dependents launch (so
+// at most one waiting grid sits behind a running one).  For a kernel launched
+// the plain way both instructions do nothing.  HBTU_LAUNCH_OVERLAP=0 in the
+// environment launches everything the plain way.
+#define HBTU_KERNEL_PROLOGUE()                                       \
+  do {                                                               \
+    asm volatile("griddepcontrol.wait;" ::: "memory");               \
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); \
+  } while (0)
+
+bool launch_overlap();  // false when HBTU_LAUNCH_OVERLAP=0 (read once)
+
+// kernel<<<grid, block, smem, st>>>(args...) with programmatic stream
+// serialisation; only for kernels that open with HBTU_KERNEL_PROLOGUE.
+template <typename... P, typename... A>
+inline void launch_k(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     A... args)
+{
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = launch_overlap() ? 1 : 0;
+  HBTU_CUDA(cudaLaunchKernelEx(&cfg, kernel, args...));
+}
+
+
 // ---------------- primitives (prims.cu) ----------------
 // Exclusive scan of n int64 values (in may equal out).  tmp: scan_tmp_bytes(n).
 size_t scan_tmp_bytes(long long n);

@@ -168,6 +168,7 @@ __device__ void plan_scan4(int S, const Ctx &c, int *out0, int *out1, int *out2,
 __global__ void k_init(Ctx c, const float *pos, const float *vel, const float *mass,
                        const long long *id)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.N) return;
   const int s = upper_bound_i(c.seg_off, c.S + 1, i) - 1;
@@ -243,6 +244,7 @@ __device__ __forceinline__ int4 counts_of(const Ctx &c, int s)
 
 __global__ void k_plan_gather(Ctx c, int mode)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= c.S) return;
   if (mode == 0) {
@@ -281,6 +283,7 @@ __device__ int get_cnt2(const Ctx &c, int s, int *v)
 
 __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode, int gathered)
 {
+  HBTU_KERNEL_PROLOGUE();
   __shared__ int tot[4];
   __shared__ int nact;
   if (threadIdx.x == 0) nact = 0;
@@ -361,6 +364,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode, int gath
 // part_info[8s+]: 0 nPos, 1 nNeg, 2 firstF, 3 firstG, 4 m_b, 5 m_f, 6 void, 7 Nbound
 __global__ void __launch_bounds__(kLB) k_part_codes(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int p = blockIdx.x * kLB + threadIdx.x;
   if (p > c.N) return;
   if (p == c.N) {
@@ -387,6 +391,7 @@ __device__ __forceinline__ int hi32(long long x) { return (int)(x >> 32); }
 
 __global__ void __launch_bounds__(kLB) k_part_pq(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int p = blockIdx.x * kLB + threadIdx.x;
   if (p >= c.N) return;
   const int s = c.pseg[p];
@@ -406,6 +411,7 @@ __global__ void __launch_bounds__(kLB) k_part_pq(Ctx c)
 
 __global__ void __launch_bounds__(kLB) k_part_fg(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int p = blockIdx.x * kLB + threadIdx.x;
   if (p >= c.N) return;
   const int s = c.pseg[p];
@@ -424,6 +430,7 @@ __global__ void __launch_bounds__(kLB) k_part_fg(Ctx c)
 
 __global__ void k_part_seg(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= c.S) return;
   const SegState &sg = c.seg[s];
@@ -452,6 +459,7 @@ __global__ void k_part_seg(Ctx c)
 
 __global__ void __launch_bounds__(kLB) k_part_gather(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int p = blockIdx.x * kLB + threadIdx.x;
   if (p >= c.N) return;
   const int s = c.pseg[p];
@@ -481,6 +489,7 @@ __global__ void __launch_bounds__(kLB) k_part_gather(Ctx c)
 
 __global__ void __launch_bounds__(kLB) k_part_copyback(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int p = blockIdx.x * kLB + threadIdx.x;
   if (p >= c.N) return;
   const SegState &sg = c.seg[c.pseg[p]];
@@ -494,6 +503,7 @@ __global__ void __launch_bounds__(kLB) k_part_copyback(Ctx c)
 // ---------------------------------------------------------------- averages
 __global__ void __launch_bounds__(kLB) k_avg_chunks(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int b = blockIdx.x;
   if (b >= c.bchunk_base[c.S]) return;
   const int s = upper_bound_i(c.bchunk_base, c.S + 1, b) - 1;
@@ -530,6 +540,7 @@ __global__ void __launch_bounds__(kLB) k_avg_chunks(Ctx c)
 // ---------------------------------------------------------------- control
 __global__ void k_control(Ctx c, int max_passes)
 {
+  HBTU_KERNEL_PROLOGUE();
   // one warp per subhalo: lanes 0..6 add the 7 chunk sums in chunk order
   // (each an independent chain), lane 0 then takes the decisions
   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -652,6 +663,7 @@ __device__ __forceinline__ bool block_of(const SegState &sg, int which, int &lo,
 
 __global__ void __launch_bounds__(kLB) k_blk_gather(Ctx c, int which)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int p = blockIdx.x * kLB + threadIdx.x;
   if (p >= c.N) return;
   const int s = c.pseg[p];
@@ -668,6 +680,7 @@ __global__ void __launch_bounds__(kLB) k_blk_gather(Ctx c, int which)
 
 __global__ void __launch_bounds__(kLB) k_blk_scatter(Ctx c, int which, int total)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kLB + threadIdx.x;
   if (e >= total) return;
   const int s = c.sb.hi_a[e];
@@ -682,6 +695,7 @@ __global__ void __launch_bounds__(kLB) k_blk_scatter(Ctx c, int which, int total
 
 __global__ void __launch_bounds__(kLB) k_blk_copyback(Ctx c, int which, int total)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kLB + threadIdx.x;
   if (e >= total) return;
   const int s = c.sb.hi_a[e];
@@ -700,6 +714,7 @@ __global__ void __launch_bounds__(kLB) k_blk_copyback(Ctx c, int which, int tota
 // energies go to eR and only reorder the list (its stored energies stay).
 __global__ void k_refine_mode(Ctx c, int enter)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= c.S) return;
   SegState &sg = c.seg[s];
@@ -720,6 +735,7 @@ __global__ void k_refine_mode(Ctx c, int enter)
 
 __global__ void k_blk_clear(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= c.S) return;
   c.seg[s].ub_lo = c.seg[s].ub_hi = 0;
@@ -728,6 +744,7 @@ __global__ void k_blk_clear(Ctx c)
 // ---------------------------------------------------------------- finalize
 __global__ void __launch_bounds__(kLB) k_kin_chunks(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int b = blockIdx.x;
   if (b >= c.bchunk_base[c.S]) return;
   const int s = upper_bound_i(c.bchunk_base, c.S + 1, b) - 1;
@@ -779,6 +796,7 @@ __global__ void __launch_bounds__(kLB) k_kin_chunks(Ctx c)
 
 __global__ void k_final_seg(Ctx c, hbtu_result *res)
 {
+  HBTU_KERNEL_PROLOGUE();
   // one warp per subhalo: lanes 0..17 add the 18 chunk sums in chunk order,
   // lane 0 then writes the result
   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -863,6 +881,7 @@ __global__ void k_final_seg(Ctx c, hbtu_result *res)
 
 __global__ void __launch_bounds__(kLB) k_final_out(Ctx c, int64_t *order, float *energy)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int p = blockIdx.x * kLB + threadIdx.x;
   if (p >= c.N) return;
   const SegState &sg = c.seg[c.pseg[p]];
@@ -884,6 +903,7 @@ __global__ void __launch_bounds__(kLB) k_final_out(Ctx c, int64_t *order, float 
 // 1024-element chunk (fixed-order tree), then the chunks of each subhalo in order.
 __global__ void __launch_bounds__(kLB) k_segsum_chunks(Ctx c, const double *x)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int b = blockIdx.x;
   if (b >= c.bchunk_base[c.S]) return;
   const int s = upper_bound_i(c.bchunk_base, c.S + 1, b) - 1;
@@ -896,6 +916,7 @@ __global__ void __launch_bounds__(kLB) k_segsum_chunks(Ctx c, const double *x)
 
 __global__ void k_segsum_combine(Ctx c, double *out)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= c.S) return;
   double t = 0.;
@@ -912,6 +933,7 @@ __device__ int get_all_chunks(const Ctx &c, int s, int *v)
 
 __global__ void __launch_bounds__(kPlanThreads) k_plan_all(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   __shared__ int tot[4];
   plan_scan4<get_all_chunks>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
 }
@@ -921,20 +943,20 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_all(Ctx c)
 // ---------------------------------------------------------------- launchers
 void launch_segment_sums(Ctx &c, const double *x, double *out)
 {
-  k_plan_all<<<1, kPlanThreads, 0, c.st>>>(c);
+  launch_k(k_plan_all, 1, kPlanThreads, 0, c.st, c);
   HBTU_LAUNCHED();
   const int max_chunks = (c.N + kChunk - 1) / kChunk + c.S;
   if (max_chunks > 0) {
-    k_segsum_chunks<<<max_chunks, kLB, 0, c.st>>>(c, x);
+    launch_k(k_segsum_chunks, max_chunks, kLB, 0, c.st, c, x);
     HBTU_LAUNCHED();
   }
-  k_segsum_combine<<<nblk(c.S, 128), 128, 0, c.st>>>(c, out);
+  launch_k(k_segsum_combine, nblk(c.S, 128), 128, 0, c.st, c, out);
   HBTU_LAUNCHED();
 }
 void launch_init(Ctx &c, const float *pos, const float *vel, const float *mass,
                  const long long *id)
 {
-  k_init<<<nblk(c.N), kLB, 0, c.st>>>(c, pos, vel, mass, id);
+  launch_k(k_init, nblk(c.N), kLB, 0, c.st, c, pos, vel, mass, id);
   HBTU_LAUNCHED();
 }
 
@@ -942,27 +964,27 @@ void launch_plan(Ctx &c, int mode)
 {
   const int gathered = c.S >= kPlanGatherMin;
   if (gathered) {
-    k_plan_gather<<<nblk(c.S, 256), 256, 0, c.st>>>(c, mode);
+    launch_k(k_plan_gather, nblk(c.S, 256), 256, 0, c.st, c, mode);
     HBTU_LAUNCHED();
   }
-  k_plan<<<1, kPlanThreads, 0, c.st>>>(c, mode, gathered);
+  launch_k(k_plan, 1, kPlanThreads, 0, c.st, c, mode, gathered);
   HBTU_LAUNCHED();
 }
 
 void launch_partition(Ctx &c)
 {
-  k_part_codes<<<nblk(c.N + 1), kLB, 0, c.st>>>(c);
+  launch_k(k_part_codes, nblk(c.N + 1), kLB, 0, c.st, c);
   HBTU_LAUNCHED();
   exclusive_scan_i64(c.pcode, c.pX, c.N + 1, c.scan_tmp, c.st);
-  k_part_pq<<<nblk(c.N), kLB, 0, c.st>>>(c);
+  launch_k(k_part_pq, nblk(c.N), kLB, 0, c.st, c);
   HBTU_LAUNCHED();
-  k_part_fg<<<nblk(c.N), kLB, 0, c.st>>>(c);
+  launch_k(k_part_fg, nblk(c.N), kLB, 0, c.st, c);
   HBTU_LAUNCHED();
-  k_part_seg<<<nblk(c.S, 128), 128, 0, c.st>>>(c);
+  launch_k(k_part_seg, nblk(c.S, 128), 128, 0, c.st, c);
   HBTU_LAUNCHED();
-  k_part_gather<<<nblk(c.N), kLB, 0, c.st>>>(c);
+  launch_k(k_part_gather, nblk(c.N), kLB, 0, c.st, c);
   HBTU_LAUNCHED();
-  k_part_copyback<<<nblk(c.N), kLB, 0, c.st>>>(c);
+  launch_k(k_part_copyback, nblk(c.N), kLB, 0, c.st, c);
   HBTU_LAUNCHED();
 }
 
@@ -970,16 +992,16 @@ void launch_averages_control(Ctx &c, int max_passes)
 {
   launch_plan(c, 1);
   const int max_chunks = (c.N + kChunk - 1) / kChunk + c.S;
-  k_avg_chunks<<<max_chunks, kLB, 0, c.st>>>(c);
+  launch_k(k_avg_chunks, max_chunks, kLB, 0, c.st, c);
   HBTU_LAUNCHED();
-  k_control<<<nblk(32ll * c.S, 128), 128, 0, c.st>>>(c, max_passes);
+  launch_k(k_control, nblk(32ll * c.S, 128), 128, 0, c.st, c, max_passes);
   HBTU_LAUNCHED();
 }
 
 void launch_block_sort(Ctx &c, int total, int which)
 {
   if (total > 0) {
-    k_blk_gather<<<nblk(c.N), kLB, 0, c.st>>>(c, which);
+    launch_k(k_blk_gather, nblk(c.N), kLB, 0, c.st, c, which);
     HBTU_LAUNCHED();
     int words[8], shifts[8], np = 0;
     for (int p = 0; p < 4; p++) {
@@ -993,32 +1015,32 @@ void launch_block_sort(Ctx &c, int total, int which)
       shifts[np++] = 8 * p;
     }
     radix_sort(c.sb, total, words, shifts, np, c.st);
-    k_blk_scatter<<<nblk(total), kLB, 0, c.st>>>(c, which, total);
+    launch_k(k_blk_scatter, nblk(total), kLB, 0, c.st, c, which, total);
     HBTU_LAUNCHED();
-    k_blk_copyback<<<nblk(total), kLB, 0, c.st>>>(c, which, total);
+    launch_k(k_blk_copyback, nblk(total), kLB, 0, c.st, c, which, total);
     HBTU_LAUNCHED();
   }
   if (which == 0) {
-    k_blk_clear<<<nblk(c.S, 128), 128, 0, c.st>>>(c);
+    launch_k(k_blk_clear, nblk(c.S, 128), 128, 0, c.st, c);
     HBTU_LAUNCHED();
   }
 }
 
 void launch_refine_mode(Ctx &c, int enter)
 {
-  k_refine_mode<<<nblk(c.S, 128), 128, 0, c.st>>>(c, enter);
+  launch_k(k_refine_mode, nblk(c.S, 128), 128, 0, c.st, c, enter);
   HBTU_LAUNCHED();
 }
 
 void launch_finalize(Ctx &c, int64_t *order_out, float *energy_out, hbtu_result *res_dev)
 {
   const int max_chunks = (c.N + kChunk - 1) / kChunk + c.S;
-  k_kin_chunks<<<max_chunks, kLB, 0, c.st>>>(c);
+  launch_k(k_kin_chunks, max_chunks, kLB, 0, c.st, c);
   HBTU_LAUNCHED();
-  k_final_seg<<<nblk(32ll * c.S, 128), 128, 0, c.st>>>(c, res_dev);
+  launch_k(k_final_seg, nblk(32ll * c.S, 128), 128, 0, c.st, c, res_dev);
   HBTU_LAUNCHED();
   if (c.N > 0) {
-    k_final_out<<<nblk(c.N), kLB, 0, c.st>>>(c, order_out, energy_out);
+    launch_k(k_final_out, nblk(c.N), kLB, 0, c.st, c, order_out, energy_out);
     HBTU_LAUNCHED();
   }
 }

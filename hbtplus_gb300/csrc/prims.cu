@@ -7,11 +7,22 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <utility>
 
 namespace hbtu {
 
 thread_local long long g_launches = 0;
+
+bool launch_overlap()
+{
+  static const bool on = [] {
+    const char *v = getenv("HBTU_LAUNCH_OVERLAP");
+    return !(v && strcmp(v, "0") == 0);
+  }();
+  return on;
+}
 
 CudaError::CudaError(cudaError_t e, const char *expr, const char *file, int line) : err(e)
 {
@@ -56,6 +67,7 @@ __device__ __forceinline__ long long block_exclusive_sum(long long v, long long 
 __global__ void __launch_bounds__(kBlock) k_scan_reduce(const long long *in, long long n,
                                                         long long *sums)
 {
+  HBTU_KERNEL_PROLOGUE();
   const long long base = (long long)blockIdx.x * kTile + (long long)threadIdx.x * kItems;
   long long s = 0;
 #pragma unroll
@@ -69,6 +81,7 @@ __global__ void __launch_bounds__(kBlock) k_scan_reduce(const long long *in, lon
 __global__ void __launch_bounds__(kBlock) k_scan_apply(const long long *in, long long *out,
                                                        long long n, const long long *offs)
 {
+  HBTU_KERNEL_PROLOGUE();
   const long long base = (long long)blockIdx.x * kTile + (long long)threadIdx.x * kItems;
   long long v[kItems], s = 0;
 #pragma unroll
@@ -103,6 +116,7 @@ struct SmallSortPasses {
 __global__ void __launch_bounds__(kBlock) k_rs_small(unsigned *hi_g, unsigned long long *lo_g,
                                                      int *val_g, int n, SmallSortPasses ps)
 {
+  HBTU_KERNEL_PROLOGUE();
   extern __shared__ __align__(16) unsigned char smem[];
   // two buffers of each field: field(b) + b * kSmallN
   unsigned long long *const lo0 = (unsigned long long *)smem;
@@ -219,6 +233,7 @@ __global__ void __launch_bounds__(kBlock) k_os_hist(const unsigned *hi,
                                                     const unsigned long long *lo, long long n,
                                                     Passes ps, unsigned *ghist)
 {
+  HBTU_KERNEL_PROLOGUE();
   __shared__ unsigned h[kMaxPasses][256];
   for (int p = 0; p < ps.n; p++) h[p][threadIdx.x] = 0;
   __syncthreads();
@@ -238,6 +253,7 @@ __global__ void __launch_bounds__(kBlock) k_os_hist(const unsigned *hi,
 __global__ void __launch_bounds__(kBlock) k_os_offsets(const unsigned *ghist, int npasses,
                                                        unsigned *goff)
 {
+  HBTU_KERNEL_PROLOGUE();
   __shared__ unsigned wsum[kBlock / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int p = 0; p < npasses; p++) {
@@ -262,6 +278,7 @@ __global__ void __launch_bounds__(kBlock) k_os_pass(
     unsigned long long *lo_out, int *val_out, long long n, int word, int shift,
     const unsigned *goff, unsigned *status, int *tile_counter, int *err)
 {
+  HBTU_KERNEL_PROLOGUE();
   __shared__ unsigned wcnt[kBlock / 32][256];
   __shared__ unsigned run_base[256];
   __shared__ unsigned hist[256];
@@ -404,16 +421,16 @@ void exclusive_scan_i64(const long long *in, long long *out, long long n, void *
   if (n <= 0) return;
   const long long nb = (n + kTile - 1) / kTile;
   if (nb == 1) {
-    k_scan_apply<<<1, kBlock, 0, st>>>(in, out, n, nullptr);
+    launch_k(k_scan_apply, 1, kBlock, 0, st, in, out, n, nullptr);
     HBTU_LAUNCHED();
     return;
   }
   long long *sums = (long long *)tmp;
   char *rest = (char *)tmp + (((size_t)nb * sizeof(long long) + 255) / 256) * 256;
-  k_scan_reduce<<<(unsigned)nb, kBlock, 0, st>>>(in, n, sums);
+  launch_k(k_scan_reduce, (unsigned)nb, kBlock, 0, st, in, n, sums);
   HBTU_LAUNCHED();
   exclusive_scan_i64(sums, sums, nb, rest, st);
-  k_scan_apply<<<(unsigned)nb, kBlock, 0, st>>>(in, out, n, sums);
+  launch_k(k_scan_apply, (unsigned)nb, kBlock, 0, st, in, out, n, sums);
   HBTU_LAUNCHED();
 }
 
@@ -438,7 +455,7 @@ void radix_sort(SortBuffers &b, long long n, const int *words, const int *shifts
       ps.words[p] = words[p];
       ps.shifts[p] = shifts[p];
     }
-    k_rs_small<<<1, kBlock, kSmallSortSmem, st>>>(b.hi_a, b.lo_a, b.val_a, (int)n, ps);
+    launch_k(k_rs_small, 1, kBlock, kSmallSortSmem, st, b.hi_a, b.lo_a, b.val_a, (int)n, ps);
     HBTU_LAUNCHED();
     return;
   }
@@ -454,14 +471,14 @@ void radix_sort(SortBuffers &b, long long n, const int *words, const int *shifts
   // global digit counts of every pass, their offsets, then one kernel per pass
   HBTU_CUDA(cudaMemsetAsync(b.os_ghist, 0, sizeof(unsigned) * 256 * kMaxPasses, st));
   const unsigned hblocks = (unsigned)std::min<long long>(ntiles, 152 * 4);
-  k_os_hist<<<hblocks, kBlock, 0, st>>>(b.hi_a, b.lo_a, n, ps, b.os_ghist);
+  launch_k(k_os_hist, hblocks, kBlock, 0, st, b.hi_a, b.lo_a, n, ps, b.os_ghist);
   HBTU_LAUNCHED();
-  k_os_offsets<<<1, kBlock, 0, st>>>(b.os_ghist, npasses, b.os_goff);
+  launch_k(k_os_offsets, 1, kBlock, 0, st, b.os_ghist, npasses, b.os_goff);
   HBTU_LAUNCHED();
   for (int p = 0; p < npasses; p++) {
     HBTU_CUDA(cudaMemsetAsync(b.os_status, 0, sizeof(unsigned) * 256 * ntiles + 64, st));
     int *tiles = reinterpret_cast<int *>(b.os_status + 256 * ntiles);
-    k_os_pass<<<(unsigned)ntiles, kBlock, 0, st>>>(b.hi_a, b.lo_a, b.val_a, b.hi_b, b.lo_b,
+    launch_k(k_os_pass, (unsigned)ntiles, kBlock, 0, st, b.hi_a, b.lo_a, b.val_a, b.hi_b, b.lo_b,
                                                    b.val_b, n, words[p], shifts[p],
                                                    b.os_goff + 256 * p, b.os_status, tiles,
                                                    b.error);

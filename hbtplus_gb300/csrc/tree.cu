@@ -31,6 +31,7 @@ constexpr int kLevelSyncMin = 1 << 18;  // tree particles from which moments go 
 
 __global__ void __launch_bounds__(kTB) k_bbox_chunks(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int b = blockIdx.x;
   const int total = c.tchunk_base[c.S];
   if (b >= total) return;
@@ -134,6 +135,7 @@ __device__ __forceinline__ bool float_fixed(float x, int E, long long &X)
 // (the len halving rule of src/gravity_tree.cpp:37-40).
 __global__ void k_cube(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= c.S) return;
   SegState &sg = c.seg[s];
@@ -173,6 +175,7 @@ __global__ void k_cube(Ctx c)
 // reference's comparisons against centres halved in double.  Left-aligned.
 __global__ void __launch_bounds__(kTB) k_keys(Ctx c, int ntotal)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kTB + threadIdx.x;
   if (e >= ntotal) return;
   const int s = upper_bound_i(c.tree_base, c.S + 1, e) - 1;
@@ -237,6 +240,7 @@ __device__ __forceinline__ int kdelta(const unsigned long long *keys, int n, int
 // Child codes: internal node -> its element index; leaf -> ~element index.
 __global__ void __launch_bounds__(kTB) k_karras(Ctx c, int ntotal)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kTB + threadIdx.x;
   if (e >= ntotal) return;
   const int s = c.sb.hi_a[e];
@@ -292,6 +296,7 @@ __device__ __forceinline__ int octant_at(unsigned long long key, int k)
 // parent's (the root always is).  Record depth bits per first key.
 __global__ void __launch_bounds__(kTB) k_cells(Ctx c, int ntotal)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kTB + threadIdx.x;
   if (e >= ntotal) return;
   const int s = c.sb.hi_a[e];
@@ -311,6 +316,7 @@ __global__ void __launch_bounds__(kTB) k_cells(Ctx c, int ntotal)
 
 __global__ void __launch_bounds__(kTB) k_popc(Ctx c, int ntotal)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kTB + threadIdx.x;
   if (e > ntotal) return;
   c.pcode[e] = e < ntotal ? __popcll(c.mask[e]) : 0;
@@ -342,6 +348,7 @@ __device__ __forceinline__ float4 make_rel(float4 a, const float fc[3], const De
 // Particle leaves: preorder index = j + #cells starting at or before key j.
 __global__ void __launch_bounds__(kTB) k_leaves(Ctx c, int ntotal)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kTB + threadIdx.x;
   if (e >= ntotal) return;
   const int s = c.sb.hi_a[e];
@@ -382,6 +389,7 @@ __global__ void __launch_bounds__(kTB) k_leaves(Ctx c, int ntotal)
 // and a count of child cells on the parent.
 __global__ void __launch_bounds__(kTB) k_cellnodes(Ctx c, int ntotal)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kTB + threadIdx.x;
   if (e >= ntotal) return;
   if (!c.iscell[e]) {
@@ -442,6 +450,7 @@ __device__ __forceinline__ void add_child(const Ctx &c, int k, double &m, double
 
 __global__ void __launch_bounds__(kTB) k_moments(Ctx c, int ntotal)
 {
+  HBTU_KERNEL_PROLOGUE();
   int e = blockIdx.x * kTB + threadIdx.x;
   if (e >= ntotal || !c.iscell[e] || c.pending0[e] != 0) return;
   c.nd[c.cidx[e]].m.x |= (int)0x80000000;
@@ -486,6 +495,7 @@ constexpr int kDepthBins = 32;  // octal depths 0 .. kMaxLevels
 
 __global__ void __launch_bounds__(kTB) k_depth_count(Ctx c, int ntotal)
 {
+  HBTU_KERNEL_PROLOGUE();
   __shared__ int h[kDepthBins];
   if (threadIdx.x < kDepthBins) h[threadIdx.x] = 0;
   __syncthreads();
@@ -498,6 +508,7 @@ __global__ void __launch_bounds__(kTB) k_depth_count(Ctx c, int ntotal)
 // lvl[0..31] counts per depth, lvl[32..63] list start per depth, lvl[64..95] cursors
 __global__ void __launch_bounds__(kTB) k_depth_fill(Ctx c, int ntotal)
 {
+  HBTU_KERNEL_PROLOGUE();
   __shared__ int h[kDepthBins], start[kDepthBins];
   if (threadIdx.x < kDepthBins) h[threadIdx.x] = 0;
   __syncthreads();
@@ -520,6 +531,7 @@ __global__ void __launch_bounds__(kTB) k_depth_fill(Ctx c, int ntotal)
 
 __global__ void __launch_bounds__(kTB) k_moments_level(Ctx c, int depth)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int count = c.lvl[depth], first = c.lvl[kDepthBins + depth];
   for (int i = blockIdx.x * kTB + threadIdx.x; i < count; i += gridDim.x * kTB) {
     const int e = c.cell_list[first + i];
@@ -556,9 +568,9 @@ inline unsigned nblk(long long n) { return (unsigned)((n + kTB - 1) / kTB); }
 
 void launch_bbox_cube(Ctx &c, int max_chunks)
 {
-  if (max_chunks > 0) k_bbox_chunks<<<max_chunks, kTB, 0, c.st>>>(c);
+  if (max_chunks > 0) launch_k(k_bbox_chunks, max_chunks, kTB, 0, c.st, c);
   HBTU_LAUNCHED();
-  k_cube<<<(c.S + 127) / 128, 128, 0, c.st>>>(c);
+  launch_k(k_cube, (c.S + 127) / 128, 128, 0, c.st, c);
   HBTU_LAUNCHED();
 }
 
@@ -566,7 +578,7 @@ void launch_tree_build(Ctx &c, const PassPlan &pl)
 {
   const int n = pl.ntree_total;
   if (n <= 0) return;
-  k_keys<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  launch_k(k_keys, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
   // LSD passes: octal-key digits (top 3*levels bits), then subhalo index
   int words[16], shifts[16], np = 0;
@@ -586,30 +598,30 @@ void launch_tree_build(Ctx &c, const PassPlan &pl)
   HBTU_CUDA(cudaMemsetAsync(c.mask, 0, sizeof(unsigned long long) * (size_t)n, c.st));
   HBTU_CUDA(cudaMemsetAsync(c.pending, 0, sizeof(int) * (size_t)n, c.st));
   HBTU_CUDA(cudaMemsetAsync(c.cslot, 0xff, sizeof(int) * 8 * (size_t)n, c.st));
-  k_karras<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  launch_k(k_karras, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
-  k_cells<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  launch_k(k_cells, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
-  k_popc<<<nblk(n + 1), kTB, 0, c.st>>>(c, n);
+  launch_k(k_popc, nblk(n + 1), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
   exclusive_scan_i64(c.pcode, c.X, n + 1, c.scan_tmp, c.st);
-  k_leaves<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  launch_k(k_leaves, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
-  k_cellnodes<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  launch_k(k_cellnodes, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
   if (n < kLevelSyncMin) {  // small trees: one launch, climbing by atomic countdown
     HBTU_CUDA(cudaMemcpyAsync(c.pending0, c.pending, sizeof(int) * (size_t)n,
                               cudaMemcpyDeviceToDevice, c.st));
-    k_moments<<<nblk(n), kTB, 0, c.st>>>(c, n);
+    launch_k(k_moments, nblk(n), kTB, 0, c.st, c, n);
     HBTU_LAUNCHED();
   } else {  // large trees: dense per-depth cell lists, one launch per depth
     HBTU_CUDA(cudaMemsetAsync(c.lvl, 0, sizeof(int) * 3 * kDepthBins, c.st));
-    k_depth_count<<<nblk(n), kTB, 0, c.st>>>(c, n);
+    launch_k(k_depth_count, nblk(n), kTB, 0, c.st, c, n);
     HBTU_LAUNCHED();
-    k_depth_fill<<<nblk(n), kTB, 0, c.st>>>(c, n);
+    launch_k(k_depth_fill, nblk(n), kTB, 0, c.st, c, n);
     HBTU_LAUNCHED();
     for (int d = pl.max_levels; d >= 0; d--) {
-      k_moments_level<<<152 * 2, kTB, 0, c.st>>>(c, d);
+      launch_k(k_moments_level, 152 * 2, kTB, 0, c.st, c, d);
       HBTU_LAUNCHED();
     }
   }
@@ -631,6 +643,7 @@ namespace {
 // empty slots keep 0)
 __global__ void __launch_bounds__(kTB) k_sib_count(Ctx c, int ntotal)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kTB + threadIdx.x;
   if (e >= ntotal || !c.iscell[e]) return;
   const int s = c.sb.hi_a[e];
@@ -651,6 +664,7 @@ __global__ void __launch_bounds__(kTB) k_sib_count(Ctx c, int ntotal)
 // the cells before it in preorder
 __global__ void __launch_bounds__(kTB) k_sib_assign(Ctx c, int ntotal)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kTB + threadIdx.x;
   if (e >= ntotal || !c.iscell[e]) return;
   const int s = c.sb.hi_a[e];
@@ -672,6 +686,7 @@ __global__ void __launch_bounds__(kTB) k_sib_assign(Ctx c, int ntotal)
 // a segment of one particle has no cell records: its two nodes keep their slots
 __global__ void k_sib_single(Ctx c)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= c.S) return;
   const SegState &sg = c.seg[s];
@@ -684,6 +699,7 @@ __global__ void k_sib_single(Ctx c)
 // every live node slot: its record at its new slot, pointers renumbered
 __global__ void __launch_bounds__(kTB) k_sib_copy(Ctx c, int nslots)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int d = blockIdx.x * kTB + threadIdx.x;
   if (d >= nslots) return;
   const int s = upper_bound_i(c.tree_base, c.S + 1, d >> 1) - 1;
@@ -710,14 +726,14 @@ void launch_sibling_layout(Ctx &c, const PassPlan &pl)
   const int nslots = 2 * n;
   HBTU_CUDA(cudaMemsetAsync(c.X2, 0, sizeof(long long) * (size_t)(nslots + 1), c.st));
   HBTU_CUDA(cudaMemsetAsync(c.newidx, 0xff, sizeof(int) * (size_t)nslots, c.st));  // -1
-  k_sib_count<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  launch_k(k_sib_count, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
   exclusive_scan_i64(c.X2, c.X2, nslots + 1, c.scan_tmp2, c.st);
-  k_sib_assign<<<nblk(n), kTB, 0, c.st>>>(c, n);
+  launch_k(k_sib_assign, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
-  k_sib_single<<<(c.S + 127) / 128, 128, 0, c.st>>>(c);
+  launch_k(k_sib_single, (c.S + 127) / 128, 128, 0, c.st, c);
   HBTU_LAUNCHED();
-  k_sib_copy<<<nblk(nslots), kTB, 0, c.st>>>(c, nslots);
+  launch_k(k_sib_copy, nblk(nslots), kTB, 0, c.st, c, nslots);
   HBTU_LAUNCHED();
 }
 

@@ -210,6 +210,7 @@ __device__ __forceinline__ void interact(float4 na, float r2, float &pot_f, floa
 template <bool kLeafRuns>
 __global__ void __launch_bounds__(kWB) k_walk_fp32(Ctx c, int total)
 {
+  HBTU_KERNEL_PROLOGUE();
   const DevParams &P = c.P;
   const unsigned full = 0xffffffffu;
   Target t;
@@ -324,6 +325,7 @@ constexpr float kBandRatio = 1.0000200002f;  // (1 + 1e-5) / (1 - 1e-5), rounded
 template <int kB, bool kSib>
 __global__ void __launch_bounds__(kB) k_walk_fp32_lean(Ctx c, int total)
 {
+  HBTU_KERNEL_PROLOGUE();
   const DevParams &P = c.P;
   Target t;
   load_target<true>(c, blockIdx.x * kB + threadIdx.x, total, t);
@@ -372,16 +374,17 @@ template <bool kSib>
 void launch_lean(Ctx &c, int n)
 {
   if (n >= 152 * 4 * 512)  // blocks of neighbouring targets share an SM's L1
-    k_walk_fp32_lean<512, kSib><<<(n + 511) / 512, 512, 0, c.st>>>(c, n);
+    launch_k(k_walk_fp32_lean<512, kSib>, (n + 511) / 512, 512, 0, c.st, c, n);
   else if (n >= 152 * 4 * 256)
-    k_walk_fp32_lean<256, kSib><<<(n + 255) / 256, 256, 0, c.st>>>(c, n);
+    launch_k(k_walk_fp32_lean<256, kSib>, (n + 255) / 256, 256, 0, c.st, c, n);
   else
-    k_walk_fp32_lean<128, kSib><<<(n + 127) / 128, 128, 0, c.st>>>(c, n);
+    launch_k(k_walk_fp32_lean<128, kSib>, (n + 127) / 128, 128, 0, c.st, c, n);
 }
 
 // FP64: the reference's arithmetic, operation by operation.
 __global__ void __launch_bounds__(kWB) k_walk_fp64(Ctx c, int total)
 {
+  HBTU_KERNEL_PROLOGUE();
   const DevParams &P = c.P;
   const unsigned full = 0xffffffffu;
   Target t;
@@ -449,6 +452,7 @@ __global__ void __launch_bounds__(kWB) k_walk_fp64(Ctx c, int total)
 // with wp' the derivative of the cubic-spline kernel; dx = x_node - x_target.
 __global__ void __launch_bounds__(kWB) k_grad_walk(Ctx c, int total)
 {
+  HBTU_KERNEL_PROLOGUE();
   const DevParams &P = c.P;
   const unsigned full = 0xffffffffu;
   Target t;
@@ -539,11 +543,11 @@ void launch_walk(Ctx &c, const PassPlan &pl)
   if (n <= 0) return;
   const unsigned blocks = (n + kWB - 1) / kWB;
   if (c.P.precision == HBTU_PRECISION_FP64)
-    k_walk_fp64<<<blocks, kWB, 0, c.st>>>(c, n);
+    launch_k(k_walk_fp64, blocks, kWB, 0, c.st, c, n);
   else if (c.opt_schedule == 1 && c.opt_leaf_runs)
-    k_walk_fp32<true><<<blocks, kWB, 0, c.st>>>(c, n);
+    launch_k(k_walk_fp32<true>, blocks, kWB, 0, c.st, c, n);
   else if (c.opt_schedule == 1)
-    k_walk_fp32<false><<<blocks, kWB, 0, c.st>>>(c, n);
+    launch_k(k_walk_fp32<false>, blocks, kWB, 0, c.st, c, n);
   else if (sibling_walk(c, pl))  // the tree build made the sibling-block records
     launch_lean<true>(c, n);
   else
@@ -555,7 +559,7 @@ void launch_grad_walk(Ctx &c, const PassPlan &pl)
 {
   const int n = pl.ntgt_total;
   if (n <= 0) return;
-  k_grad_walk<<<(n + kWB - 1) / kWB, kWB, 0, c.st>>>(c, n);
+  launch_k(k_grad_walk, (n + kWB - 1) / kWB, kWB, 0, c.st, c, n);
   HBTU_LAUNCHED();
 }
 
