@@ -22,6 +22,7 @@ __global__ void __launch_bounds__(kDT) k_direct_fp64(const float4 *pm, int n, co
                                                      int nt, int nsplit, double *partial,
                                                      DevParams P)
 {
+  HBTU_KERNEL_PROLOGUE();
   __shared__ float4 src[kSrcTile];
   const int t = blockIdx.x * kDT + threadIdx.x;
   const int split = blockIdx.y;
@@ -70,6 +71,7 @@ __global__ void __launch_bounds__(kDT) k_direct_fp64(const float4 *pm, int n, co
 __global__ void k_direct_reduce(const double *partial, int nt, int nsplit, double *out,
                                 DevParams P)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nt) return;
   double s = 0.;
@@ -84,9 +86,9 @@ void direct_potential_fp64(const DevParams &P, const float4 *pm, int n, const in
 {
   if (nt <= 0) return;
   dim3 grid((nt + kDT - 1) / kDT, nsplit);
-  k_direct_fp64<<<grid, kDT, 0, st>>>(pm, n, tidx, nt, nsplit, partial, P);
+  launch_k(k_direct_fp64, grid, kDT, 0, st, pm, n, tidx, nt, nsplit, partial, P);
   HBTU_LAUNCHED();
-  k_direct_reduce<<<(nt + 255) / 256, 256, 0, st>>>(partial, nt, nsplit, out, P);
+  launch_k(k_direct_reduce, (nt + 255) / 256, 256, 0, st, partial, nt, nsplit, out, P);
   HBTU_LAUNCHED();
 }
 

@@ -49,6 +49,7 @@ constexpr unsigned long long kSign = 0x8000000000000000ull;  // signed -> unsign
 __global__ void __launch_bounds__(kIB) k_ix_minmax(const int64_t *keys, int64_t n,
                                                    unsigned long long *mm)
 {
+  HBTU_KERNEL_PROLOGUE();
   unsigned long long lo = ~0ull, hi = 0ull;
   for (int64_t i = (int64_t)blockIdx.x * kIB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kIB) {
     const unsigned long long b = (unsigned long long)keys[i] ^ kSign;
@@ -81,6 +82,7 @@ __device__ __forceinline__ unsigned long long ix_hash(unsigned long long x)
 __global__ void __launch_bounds__(kIB) k_ix_hash_fill(const int64_t *keys, int64_t n, int *hslot,
                                                       unsigned long long mask)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int64_t i = (int64_t)blockIdx.x * kIB + threadIdx.x;
   if (i >= n) return;
   const long long k = keys[i];
@@ -99,6 +101,7 @@ __global__ void __launch_bounds__(kIB) k_ix_hash_fill(const int64_t *keys, int64
 
 __global__ void __launch_bounds__(kIB) k_ix_flat_clear(int *dense, int64_t span)
 {
+  HBTU_KERNEL_PROLOGUE();
   for (int64_t i = (int64_t)blockIdx.x * kIB + threadIdx.x; i < span;
        i += (int64_t)gridDim.x * kIB)
     dense[i] = -1;
@@ -107,6 +110,7 @@ __global__ void __launch_bounds__(kIB) k_ix_flat_clear(int *dense, int64_t span)
 __global__ void __launch_bounds__(kIB) k_ix_flat_fill(const int64_t *keys, int64_t n, int64_t kmin,
                                                       int *dense)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int64_t i = (int64_t)blockIdx.x * kIB + threadIdx.x;
   if (i >= n) return;
   atomicMax(&dense[(unsigned long long)keys[i] - (unsigned long long)kmin], (int)i);
@@ -119,6 +123,7 @@ __global__ void __launch_bounds__(kIB) k_ix_lookup_mapped(const int64_t *keys, c
                                                           int64_t null_index, const int64_t *q,
                                                           int64_t m, int64_t *out)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int64_t j = (int64_t)blockIdx.x * kIB + threadIdx.x;
   if (j >= m) return;
   const int64_t key = q[j];
@@ -143,6 +148,7 @@ __global__ void __launch_bounds__(kIB) k_ix_lookup_flat(const int *dense, const 
                                                         int64_t null_index, const int64_t *q,
                                                         int64_t m, int64_t *out)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int64_t j = (int64_t)blockIdx.x * kIB + threadIdx.x;
   if (j >= m) return;
   const int64_t key = q[j];
@@ -274,7 +280,7 @@ hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int6
     // pass 1: key range (one small read back)
     const unsigned long long init[2] = {~0ull, 0ull};
     HBTU_CUDA(cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, st));
-    k_ix_minmax<<<std::min<int64_t>(iblk(n), 152 * 8), kIB, 0, st>>>(ksrc, n, mm);
+    launch_k(k_ix_minmax, std::min<int64_t>(iblk(n), 152 * 8), kIB, 0, st, ksrc, n, mm);
     HBTU_LAUNCHED();
     unsigned long long hmm[2];
     HBTU_CUDA(cudaMemcpyAsync(hmm, mm, sizeof(hmm), cudaMemcpyDeviceToHost, st));
@@ -294,10 +300,11 @@ hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int6
       t->values = reinterpret_cast<int64_t *>(t->mem);
       t->dense = reinterpret_cast<int *>(t->mem + bvals);
       HBTU_CUDA(cudaMemcpyAsync(t->values, vsrc, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, st));
-      k_ix_flat_clear<<<(unsigned)std::min<unsigned long long>((span + kIB - 1) / kIB, 152 * 16),
-                        kIB, 0, st>>>(t->dense, (int64_t)span);
+      launch_k(k_ix_flat_clear,
+               (unsigned)std::min<unsigned long long>((span + kIB - 1) / kIB, 152 * 16), kIB, 0, st,
+               t->dense, (int64_t)span);
       HBTU_LAUNCHED();
-      k_ix_flat_fill<<<iblk(n), kIB, 0, st>>>(ksrc, n, t->kmin, t->dense);
+      launch_k(k_ix_flat_fill, iblk(n), kIB, 0, st, ksrc, n, t->kmin, t->dense);
       HBTU_LAUNCHED();
     } else {
       // hash slots: a power of two at least twice the pairs
@@ -315,7 +322,7 @@ hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int6
       HBTU_CUDA(cudaMemcpyAsync(t->values, vsrc, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, st));
       HBTU_CUDA(cudaMemcpyAsync(t->keys, ksrc, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, st));
       HBTU_CUDA(cudaMemsetAsync(t->hslot, 0xff, sizeof(int) * slots, st));  // -1: free
-      k_ix_hash_fill<<<iblk(n), kIB, 0, st>>>(t->keys, n, t->hslot, t->hmask);
+      launch_k(k_ix_hash_fill, iblk(n), kIB, 0, st, t->keys, n, t->hslot, t->hmask);
       HBTU_LAUNCHED();
       HBTU_CUDA(cudaStreamSynchronize(st));
     }
@@ -350,11 +357,12 @@ hbtu_status hbtu_index_lookup(hbtu_index_table *t, const int64_t *keys, int64_t 
       dq = sq;
     }
     if (t->flat)
-      k_ix_lookup_flat<<<iblk(m), kIB, 0, st>>>(t->dense, t->values, t->n, t->kmin, t->kmax,
-                                                t->null_index, dq, m, dout);
+      launch_k(k_ix_lookup_flat, iblk(m), kIB, 0, st, t->dense, t->values, t->n, t->kmin, t->kmax,
+               t->null_index, dq, m, dout);
     else
-      k_ix_lookup_mapped<<<iblk(m), kIB, 0, st>>>(t->keys, t->hslot, t->values, t->hmask, t->n,
-                                                  t->kmin, t->kmax, t->null_index, dq, m, dout);
+      launch_k(k_ix_lookup_mapped, iblk(m), kIB, 0, st,
+               t->keys, t->hslot, t->values, t->hmask, t->n,
+               t->kmin, t->kmax, t->null_index, dq, m, dout);
     HBTU_LAUNCHED();
     if (host) {
       HBTU_CUDA(cudaMemcpyAsync(out, dout, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, st));

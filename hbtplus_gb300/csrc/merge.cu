@@ -64,6 +64,7 @@ __device__ void core_moments(const float *x, const float *mass, int64_t np, bool
 __global__ void k_cores(const MergeSeg *seg, int64_t S, const float *pos, const float *vel,
                         const float *mass, hbtu_core *cores, DevParams P)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= S) return;
   const MergeSeg g = seg[s];
@@ -108,6 +109,7 @@ __global__ void k_traps(const MergeSeg *seg, int64_t S, const hbtu_core *cores,
                         const float *mb_pos, const float *mb_vel, int isnap, long long *sink,
                         int *sink_snap, int *merged, int *error, DevParams P)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= S || sink[s] >= 0) return;  // IsTrapped already
   const float mbp[3] = {mb_pos[3 * s], mb_pos[3 * s + 1], mb_pos[3 * s + 2]};
@@ -213,10 +215,10 @@ extern "C" hbtu_status hbtu_merge_detect(hbtu_handle *h, const hbtu_particles *p
     HBTU_CUDA(cudaMemsetAsync(d_merged, 0, 4 * nsub, st));
     HBTU_CUDA(cudaMemsetAsync(d_err, 0, 4, st));
     const unsigned blocks = (unsigned)((nsub + 127) / 128);
-    k_cores<<<blocks, 128, 0, st>>>(d_seg, nsub, d_pos, d_vel, d_mass, d_core, h->dp);
+    launch_k(k_cores, blocks, 128, 0, st, d_seg, nsub, d_pos, d_vel, d_mass, d_core, h->dp);
     HBTU_LAUNCHED();
-    k_traps<<<blocks, 128, 0, st>>>(d_seg, nsub, d_core, d_mbp, d_mbv, snapshot_index, d_sink,
-                                    d_snap, d_merged, d_err, h->dp);
+    launch_k(k_traps, blocks, 128, 0, st, d_seg, nsub, d_core, d_mbp, d_mbv, snapshot_index, d_sink,
+             d_snap, d_merged, d_err, h->dp);
     HBTU_LAUNCHED();
     int err = 0;
     HBTU_CUDA(cudaMemcpyAsync(sink, d_sink, 8 * nsub, cudaMemcpyDeviceToHost, st));

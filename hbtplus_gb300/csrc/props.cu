@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(kPB) k_pr_elem(const PropSeg *seg, const int64
                                                  const int64_t *order, unsigned long long *lo,
                                                  unsigned *hi, int *val, int *flags, DevParams P)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int64_t j = (int64_t)blockIdx.x * kPB + threadIdx.x;
   int lowbit = 0x7fffffff, highbit = -0x7fffffff;
   if (j < T) {
@@ -149,6 +150,7 @@ __global__ void __launch_bounds__(kPB) k_pr_fix(const PropSeg *seg, const int64_
                                                 const int64_t *order, const int *flags,
                                                 float *msorted, long long *mfix)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int64_t q = (int64_t)blockIdx.x * kPB + threadIdx.x;
   if (q > T) return;
   if (q == T) {
@@ -175,6 +177,7 @@ __global__ void k_pr_seq(const PropSeg *__restrict__ seg, int S, int64_t T,
                          const float *__restrict__ msorted, const int *__restrict__ flags,
                          const long long *__restrict__ cum, float *__restrict__ mc)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= S) return;
   const PropSeg g = seg[s];
@@ -214,6 +217,7 @@ __global__ void __launch_bounds__(kPB) k_pr_prof(const PropSeg *seg, const int64
                                                  float *rc, float *mc, unsigned long long *vmax,
                                                  long long *so, float *quant)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int64_t q = (int64_t)blockIdx.x * kPB + threadIdx.x;
   const int lane = threadIdx.x & 31;
   int s = -1 - lane;  // a run of its own for lanes past the end
@@ -256,6 +260,7 @@ __global__ void __launch_bounds__(kPB) k_pr_shape(const PropSeg *seg, const int 
                                                   const float *pos, const float *mass,
                                                   const int64_t *order, double *csum, DevParams P)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int b = (int)(((int64_t)blockIdx.x * kPB + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (b >= nch) return;  // whole warps leave together
@@ -309,6 +314,7 @@ __global__ void k_pr_final(const PropSeg *seg, int S, const double *csum, const 
                            const float *quant, const float *last_max, const int *last_snap,
                            int snapshot_index, float velocity_unit, hbtu_props *out)
 {
+  HBTU_KERNEL_PROLOGUE();
   const int s = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (s >= S) return;
@@ -505,8 +511,8 @@ extern "C" hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_partic
     HBTU_CUDA(cudaMemsetAsync(d_so, 0xff, 8 * nsub, st));  // -1: no radius qualifies
     HBTU_CUDA(cudaMemsetAsync(d_quant, 0, 8 * nsub, st));
     if (T > 0) {
-      k_pr_elem<<<pblk(T), kPB, 0, st>>>(d_seg, d_boff, (int)nsub, T, d_pos, d_mass, d_ord,
-                                         sb.lo_a, sb.hi_a, sb.val_a, d_flags, P);
+      launch_k(k_pr_elem, pblk(T), kPB, 0, st, d_seg, d_boff, (int)nsub, T, d_pos, d_mass, d_ord,
+               sb.lo_a, sb.hi_a, sb.val_a, d_flags, P);
       HBTU_LAUNCHED();
       // stable LSD passes: the distance's 32 bits, then the subhalo index
       int words[16], shifts[16], np = 0;
@@ -519,26 +525,25 @@ extern "C" hbtu_status hbtu_subhalo_properties(hbtu_handle *h, const hbtu_partic
         shifts[np++] = b;
       }
       radix_sort(sb, T, words, shifts, np, st);
-      k_pr_fix<<<pblk(T + 1), kPB, 0, st>>>(d_seg, d_boff, (int)nsub, T, sb.val_a, d_mass,
-                                            d_ord, d_flags, d_ms, d_mfix);
+      launch_k(k_pr_fix, pblk(T + 1), kPB, 0, st, d_seg, d_boff, (int)nsub, T, sb.val_a, d_mass,
+               d_ord, d_flags, d_ms, d_mfix);
       HBTU_LAUNCHED();
       exclusive_scan_i64(d_mfix, d_cum, T + 1, d_scan, st);
-      k_pr_seq<<<(unsigned)((nsub + 127) / 128), 128, 0, st>>>(d_seg, (int)nsub, T, d_ms,
-                                                               d_flags, d_cum, d_mc);
+      launch_k(k_pr_seq, (unsigned)((nsub + 127) / 128), 128, 0, st, d_seg, (int)nsub, T, d_ms,
+               d_flags, d_cum, d_mc);
       HBTU_LAUNCHED();
-      k_pr_prof<<<pblk(T), kPB, 0, st>>>(d_seg, d_boff, (int)nsub, T, sb.lo_a, d_mfix, d_cum,
-                                         d_flags, P.eps, rho_vir, d_rc, d_mc, d_vmax, d_so,
-                                         d_quant);
+      launch_k(k_pr_prof, pblk(T), kPB, 0, st, d_seg, d_boff, (int)nsub, T, sb.lo_a, d_mfix, d_cum,
+               d_flags, P.eps, rho_vir, d_rc, d_mc, d_vmax, d_so, d_quant);
       HBTU_LAUNCHED();
     }
     if (nch) {
-      k_pr_shape<<<(unsigned)((32 * (int64_t)nch + kPB - 1) / kPB), kPB, 0, st>>>(
-          d_seg, d_cseg, nch, d_pos, d_mass, d_ord, d_csum, P);
+      launch_k(k_pr_shape, (unsigned)((32 * (int64_t)nch + kPB - 1) / kPB), kPB, 0, st, d_seg,
+               d_cseg, nch, d_pos, d_mass, d_ord, d_csum, P);
       HBTU_LAUNCHED();
     }
-    k_pr_final<<<(unsigned)((32 * nsub + 127) / 128), 128, 0, st>>>(
-        d_seg, (int)nsub, d_csum, d_rc, d_mc, d_vmax, d_so, d_quant, d_last, d_lsnap,
-        snapshot_index, velocity_unit, d_out);
+    launch_k(k_pr_final, (unsigned)((32 * nsub + 127) / 128), 128, 0, st, d_seg, (int)nsub, d_csum,
+             d_rc, d_mc, d_vmax, d_so, d_quant, d_last, d_lsnap, snapshot_index, velocity_unit,
+             d_out);
     HBTU_LAUNCHED();
     std::vector<long long> hso(nsub);
     int hflags[F_WORDS];
