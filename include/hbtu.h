@@ -117,7 +117,12 @@ hbtu_status hbtu_destroy(hbtu_handle *h);
 /* Enqueue the handle's work on a caller-owned cudaStream_t from now on.
  * NULL is CUDA's legacy default stream (what a framework's "current stream"
  * is by default), so work there is ordered with the caller's.  A new handle
- * uses a stream of its own. */
+ * uses a stream of its own.  The library's kernels are launched with
+ * programmatic stream serialisation: each is scheduled while the kernel
+ * before it still runs, and waits (griddepcontrol.wait) for that kernel to
+ * complete before it touches memory, so stream order is kept, also after the
+ * caller's own kernels.  HBTU_LAUNCH_OVERLAP=0 in the environment launches
+ * them the plain way. */
 hbtu_status hbtu_set_stream(hbtu_handle *h, void *cuda_stream);
 
 /* Unbind one subhalo: Subhalo_t::Unbind (src/subhalo_unbind.cpp:263-431).
