@@ -280,7 +280,7 @@ hbtu_status hbtu_index_fill(hbtu_index_table *t, const int64_t *keys, const int6
     // pass 1: key range (one small read back)
     const unsigned long long init[2] = {~0ull, 0ull};
     HBTU_CUDA(cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, st));
-    launch_k(k_ix_minmax, std::min<int64_t>(iblk(n), 152 * 8), kIB, 0, st, ksrc, n, mm);
+    launch_k(k_ix_minmax, (unsigned)std::min<int64_t>(iblk(n), 152 * 8), kIB, 0, st, ksrc, n, mm);
     HBTU_LAUNCHED();
     unsigned long long hmm[2];
     HBTU_CUDA(cudaMemcpyAsync(hmm, mm, sizeof(hmm), cudaMemcpyDeviceToHost, st));
