@@ -206,6 +206,28 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def copy_times(pin, dev, outs, stream, steps):
+    """(host->device ms, device->host ms) per step: the pinned input arrays copied
+    to their device buffers, and the device outputs to pinned host buffers,
+    each bracketed by CUDA events on `stream`, averaged over `steps`."""
+    import torch
+    h2d, d2h = [], []
+    for _ in range(max(1, steps)):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        e[0].record(stream)
+        for k, v in pin.items():
+            dev[k].copy_(v, non_blocking=True)
+        e[1].record(stream)
+        for host, d in outs:
+            host.copy_(d, non_blocking=True)
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        h2d.append(e[0].elapsed_time(e[1]))
+        d2h.append(e[1].elapsed_time(e[2]))
+    return statistics.mean(h2d), statistics.mean(d2h)
+
+
 def run_reference_arm(args, ws, rank):
     if rank != 0:
         return
@@ -565,8 +587,15 @@ def main():
     h2d = sum(int(v.numel() * v.element_size()) for v in pin.values()) + offsets.nbytes + \
         C.sizeof(states)
     d2h = ntot * (8 + 4) + nsub * C.sizeof(_lib.hbtu_result)
+    h2d_ms, d2h_ms = copy_times(pin, d_in, [(out_order, d_out["order"]),
+                                            (out_energy, d_out["energy"])],
+                                stream, args.steps)
     e2e = {"value": ws * nsub / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s}
+           "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s,
+           "h2d_ms": h2d_ms, "d2h_ms": d2h_ms,
+           "copies_note": "h2d_ms / d2h_ms: the particle copies in and the order and energy "
+                          "copies out, timed alone with CUDA events (the e2e call overlaps "
+                          "nothing: its copies run on the library's stream in order)"}
 
     # -- plain form: one subhalo per call on the same GB300 ------------------------
     plain = None

@@ -56,6 +56,16 @@ hbtu_status scratch_on_current_device(char **out)
     set_global_error("hbtu_unbind_noalloc: no current CUDA device");
     return HBTU_ERR_NO_DEVICE;
   }
+  int major = 0, minor = 0;
+  if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess ||
+      major != 10 || minor != 3) {
+    cudaGetLastError();
+    set_global_error("hbtu_unbind_noalloc: device %d is not compute capability 10.3 (this "
+                     "library is built for sm_103a only)",
+                     dev);
+    return HBTU_ERR_NO_DEVICE;
+  }
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
   if (!g_scratch_ptr[dev]) {
     void *p = nullptr;
@@ -120,6 +130,7 @@ extern "C" hbtu_status hbtu_unbind_noalloc(const hbtu_params *params, const hbtu
   char *base = nullptr;
   hbtu_status rc = scratch_on_current_device(&base);
   if (rc != HBTU_OK) return rc;
+  const cudaStream_t stream = (cudaStream_t)cuda_stream;
   try {
     Ctx c;
     Staging sg;
@@ -128,7 +139,7 @@ extern "C" hbtu_status hbtu_unbind_noalloc(const hbtu_params *params, const hbtu
     c.P = derive_params(*params);
     c.N = (int)n;
     c.S = 1;
-    c.st = (cudaStream_t)cuda_stream;
+    c.st = stream;
     c.plan_host = &plan_host;
     c.pot_out = nullptr;
     c.grad_pos = c.grad_vel = c.grad_mass = nullptr;
@@ -161,6 +172,10 @@ extern "C" hbtu_status hbtu_unbind_noalloc(const hbtu_params *params, const hbtu
     return HBTU_OK;
   } catch (const CudaError &e) {
     set_global_error("%s", e.what.c_str());
+    // kernels already queued may still be writing the shared array: let them
+    // finish, so the array is idle whenever this function returns
+    cudaStreamSynchronize(stream);
+    cudaGetLastError();
     return HBTU_ERR_CUDA;
   }
 }

@@ -129,9 +129,11 @@ hbtu_status UnbindGPU(hbtu_handle *h, const hbtu_params &params, SubhaloT &sub,
   std::vector<float> energy(n > 0 ? n : 1);
   hbtu_result r;
   const hbtu_status rc = hbtu_unbind(h, &p, n, &st, order.data(), energy.data(), &r);
-  if (rc != HBTU_OK) return rc;
+  if (rc != HBTU_OK && rc != HBTU_ERR_NOT_CONVERGED) return rc;
+  // a pass cap (params.max_passes) that ends the loop early still leaves the
+  // subhalo as the last pass left it, as the batch form does
   detail::apply(sub, epoch, r, order.data(), energy.data(), energies);
-  return HBTU_OK;
+  return rc;
 }
 
 // The independent Unbind calls of one nesting level in one device call:

@@ -843,6 +843,53 @@ int hbto_binding_energies(const hbto_params *par, int64_t n, const float *pos, c
   return 0;
 }
 
+/* The potentials GravityTree_t::EvaluatePotential (src/gravity_tree.cpp:79-164)
+ * gives the particles targets[0..ntarget) from one tree over all n particles
+ * (OctTree_t::Build + UpdateInternalNodes, src/oct_tree.tpp:16-144,
+ * src/gravity_tree.cpp:18-77), self term cancelled as in the first pass of the
+ * loop (src/subhalo_unbind.cpp:341-354), for each of ntheta opening angles:
+ * the tree does not depend on the angle, so it is built once.
+ * potential[k*ntarget + j] is target j at open_angles[k]; interactions[k]
+ * (may be NULL) counts the contributions summed at that angle. */
+int hbto_tree_potentials(const hbto_params *par, int64_t n, const float *pos, const float *mass,
+                         int64_t ntarget, const int64_t *targets, int32_t ntheta,
+                         const double *open_angles, double *potential, int64_t *interactions,
+                         int nthreads)
+{
+  dpar d;
+  derive(par, &d);
+#ifdef _OPENMP
+  int nthr = nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+  int nthr = 1;
+  (void)nthreads;
+#endif
+  for (int64_t j = 0; j < ntarget; j++)
+    if (targets[j] < 0 || targets[j] >= n) return 1;
+  int64_t *pid = malloc((n > 0 ? n : 1) * sizeof(int64_t));
+  if (!pid) return 2;
+  for (int64_t i = 0; i < n; i++) pid[i] = i;
+  otree t;
+  tree_init(&t);
+  tree_build(&t, pid, n, pos, mass, 1.f, &d);
+  for (int32_t k = 0; k < ntheta; k++) {
+    hbto_params pk = *par;
+    pk.open_angle = open_angles[k];
+    dpar dk;
+    derive(&pk, &dk);
+    int64_t c = 0;
+#pragma omp parallel for reduction(+ : c) schedule(dynamic, 64) num_threads(nthr)
+    for (int64_t j = 0; j < ntarget; j++) {
+      const int64_t i = targets[j];
+      potential[(size_t)k * ntarget + j] = eval_potential(&t, pos + 3 * i, mass[i], &dk, &c);
+    }
+    if (interactions) interactions[k] = c;
+  }
+  tree_free(&t);
+  free(pid);
+  return 0;
+}
+
 void hbto_srand48(long seed) { srand48(seed); }
 
 /* ------------------------------------------------------------------ ID tables */

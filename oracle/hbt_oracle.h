@@ -104,6 +104,17 @@ int hbto_binding_energies(const hbto_params *par, int64_t n, const float *pos, c
                           const float *mass, const float ref_pos[3], const float ref_vel[3],
                           float *energy, double *potential, int64_t *interactions, int nthreads);
 
+/* EvaluatePotential (src/gravity_tree.cpp:79-164) of the particles
+ * targets[0..ntarget) (indices into pos/mass) from one tree over all n
+ * particles, self term cancelled, at each of ntheta opening angles (the tree is
+ * built once): potential[k*ntarget + j] for open_angles[k]; interactions[k]
+ * (may be NULL) counts the contributions summed.  par->open_angle is unused.
+ * Returns 0, or 1 for a target out of range. */
+int hbto_tree_potentials(const hbto_params *par, int64_t n, const float *pos, const float *mass,
+                         int64_t ntarget, const int64_t *targets, int32_t ntheta,
+                         const double *open_angles, double *potential, int64_t *interactions,
+                         int nthreads);
+
 /* The reference's Hoare-style split of an energy list
  * (PartitionBindingEnergy, src/subhalo_unbind.cpp:21-58): permutes E[] and
  * idx[] in place and returns the number of entries kept in front. */

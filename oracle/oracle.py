@@ -17,6 +17,10 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# Where the reference's sources are (the harness build and the header checks):
+# $HBTPLUS_REFERENCE, else the Makefile's default.  Absent on most hosts.
+REFERENCE_DIR = os.environ.get("HBTPLUS_REFERENCE") or subprocess.run(
+    ["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True).stdout.strip()
 ORACLE_SO = os.path.join(HERE, "_build", "libhbt_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libhbt_ref.so")
 
@@ -123,8 +127,13 @@ def make_state(ref_pos, ref_vel, mb_pos, mb_vel, mb_id) -> State:
 
 def build(reference: bool = False) -> None:
     """Compile the oracle (and, with reference=True, the reference harness)."""
-    target = ["ref"] if reference else []
+    target = ["ref", "REF=" + REFERENCE_DIR] if reference else []
     subprocess.run(["make", "-s", "-C", HERE, "-j8"] + target, check=True)
+
+
+def reference_present() -> bool:
+    """True where the reference's sources can be compiled from."""
+    return bool(REFERENCE_DIR) and os.path.isdir(os.path.join(REFERENCE_DIR, "src"))
 
 
 def _p(a, t):
@@ -430,6 +439,30 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle batch unbind failed with status {rc}")
         return order[:ntot], energy[:ntot], [result_dict(res[s]) for s in range(nsub)]
+
+    def tree_potentials(self, params: dict, pos, mass, targets, open_angles,
+                        nthreads: int = 0, drand_seed: int = 1):
+        """EvaluatePotential of the particles ``targets`` from one reference
+        tree over all particles, at each opening angle (C restatement only):
+        (potentials (len(open_angles), len(targets)), interactions per angle)."""
+        if self.reference:
+            raise ValueError("tree_potentials exists in the C restatement only")
+        f = self.lib.hbto_tree_potentials
+        n = len(mass)
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1)
+        mass = np.ascontiguousarray(mass, np.float32)
+        t = np.ascontiguousarray(targets, np.int64)
+        th = np.ascontiguousarray(open_angles, np.float64)
+        pot = np.zeros((len(th), max(len(t), 1)), np.float64)
+        cnt = np.zeros(max(len(th), 1), np.int64)
+        par = make_params(params)
+        self.srand48(drand_seed)
+        rc = f(C.byref(par), C.c_int64(n), _p(pos, C.c_float), _p(mass, C.c_float),
+               C.c_int64(len(t)), _p(t, C.c_int64), C.c_int32(len(th)), _p(th, C.c_double),
+               _p(pot, C.c_double), _p(cnt, C.c_int64), C.c_int(nthreads))
+        if rc != 0:
+            raise RuntimeError(f"oracle tree potentials failed with status {rc}")
+        return pot[:, :len(t)], cnt[:len(th)]
 
     def binding_energies(self, params: dict, pos, vel, mass, ref_pos, ref_vel,
                          nthreads: int = 1, drand_seed: int = 1):

@@ -2,8 +2,15 @@
 Mpc/h, c = 5) with 300 Plummer clumps of 1e3-1e5 particles and 5% contaminants
 (about 2.7e7 particles), unbound with opening angles 0.3, 0.45 and 0.7.
 
-Checked against exact FP64 pairwise sums (hbtu_direct_potential) on a random
-1e4-particle subsample:
+Checked on a random 1e4-particle subsample against
+  * the reference tree: the C oracle's restatement of OctTree_t::Build and
+    EvaluatePotential (pinned bit for bit to the reference's first-pass
+    potentials by tests/test_oracle.py), one tree over all 2.7e7 particles
+    evaluated at the same targets for each opening angle.  The GPU walk makes
+    the same opening decisions in FP32 on coordinates relative to the frame,
+    so its potentials must agree within 1e-5 relative (measured: about 1e-7);
+and against exact FP64 pairwise sums (hbtu_direct_potential, itself checked
+against an independent numpy FP64 pairwise sum below):
   * tree potentials of the first pass: relative error below 1e-2 at the 99th
     percentile for theta = 0.45 and growing with theta;
   * bound mass: the final bound set classified by the tree energy and by the
@@ -18,6 +25,68 @@ import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+
+def numpy_direct_potential(pos, mass, targets, p):
+    """Independent FP64 pairwise potentials: the reference's spline softening
+    (src/gravity_tree.cpp:144-160, h = 2.8 eps, exact fractions), NEAREST on
+    each coordinate difference, self term excluded, times G/a with G, a and eps
+    rounded to float as the reference stores them."""
+    eps = float(np.float32(p["softening"]))
+    h = 2.8 * eps
+    hinv = 1.0 / h
+    box = float(np.float32(p["box_size"]))
+    half = float(np.float32(box / 2.0))
+    G = float(np.float32(p["G"]))
+    a = float(np.float32(p["scale_factor"]))
+    x = np.asarray(pos, np.float32).astype(np.float64)
+    m = np.asarray(mass, np.float32).astype(np.float64)
+    out = np.empty(len(targets))
+    branches = np.zeros(3, np.int64)  # pairs with u < 0.5, 0.5 <= u < 1, r >= h
+    for j, t in enumerate(targets):
+        d = x - x[t]
+        if p["periodic"]:
+            d = np.where(d > half, d - box, np.where(d < -half, d + box, d))
+        r = np.sqrt(np.sum(d * d, axis=1))
+        u = r * hinv
+        wp_in = -2.8 + u * u * (16.0 / 3.0 + u * u * (6.4 * u - 9.6))
+        us = np.where(u > 0, u, 1.0)
+        wp_mid = -3.2 + 1.0 / (15.0 * us) + u * u * (32.0 / 3.0 + u * (-16.0 + u * (9.6 - 32.0 / 15.0 * u)))
+        k = np.where(r >= h, -1.0 / np.where(r > 0, r, 1.0), hinv * np.where(u < 0.5, wp_in, wp_mid))
+        k[t] = 0.0
+        out[j] = np.sum(m * k)
+        near = np.arange(len(m)) != t
+        branches += [np.sum(near & (u < 0.5)), np.sum(near & (u >= 0.5) & (r < h)),
+                     np.sum(near & (r >= h))]
+    return out * G / a, branches
+
+
+@pytest.mark.parametrize("periodic", [1, 0])
+def test_direct_potential_against_numpy_fp64(periodic):
+    """hbtu_direct_potential, the FP64 truth of the 2.7e7-particle checks,
+    against an independent pairwise sum: a dense clump (pairs inside both
+    spline branches) and a wide cloud, centred on a corner of the 100 Mpc/h box
+    so that the periodic wrap is taken on every axis."""
+    from hbtplus_gb300 import synthetic as S
+    from hbtplus_gb300.unbind import Unbinder
+    rng = np.random.default_rng(11 + periodic)
+    clump = rng.normal(scale=0.003, size=(3000, 3))
+    cloud = rng.uniform(-0.1, 0.1, size=(3000, 3))
+    pos = np.concatenate([clump, cloud]) + (0.0004 if periodic else 50.0)
+    if periodic:
+        pos = np.mod(pos, 100.0)
+    pos = pos.astype(np.float32)
+    mass = rng.uniform(1e-4, 3e-4, len(pos)).astype(np.float32)
+    p = S.default_params(periodic=periodic)
+    targets = np.sort(rng.choice(len(pos), 400, replace=False))
+    with Unbinder(p) as ub:
+        got = ub.direct_potential(pos, mass, targets)
+    want, branches = numpy_direct_potential(pos, mass, targets, p)
+    assert np.all(branches > 1000), branches  # every branch of the spline is exercised
+    rel = np.abs(got - want) / np.abs(want)
+    print(f"direct potential vs numpy FP64 (periodic {periodic}): max rel {rel.max():.2e}, "
+          f"pairs per branch {branches.tolist()}")
+    assert rel.max() <= 1e-12
 
 
 @pytest.fixture(scope="module")
@@ -35,14 +104,30 @@ def test_large_host_against_fp64_direct_sum(host):
     tidx = np.sort(rng.choice(n, 10_000, replace=False))
     with Unbinder(S.default_params()) as ub:
         phi_direct = ub.direct_potential(host["pos"], host["mass"], tidx)
+    # the reference tree over all particles, evaluated at the subsample
+    from oracle import Oracle
+    thetas = (0.3, 0.45, 0.7)
+    t0 = time.perf_counter()
+    phi_reftree, _ = Oracle().tree_potentials(S.default_params(), host["pos"], host["mass"],
+                                              tidx, thetas)
+    print(f"reference tree over {n} particles, {len(tidx)} targets x 3 angles: "
+          f"{time.perf_counter() - t0:.1f} s")
     p99 = {}
     results = {}
-    for theta in (0.3, 0.45, 0.7):
+    for k, theta in enumerate(thetas):
         with Unbinder(S.default_params(open_angle=theta)) as ub:
             _, pot = ub.binding_energies(host["pos"], host["vel"], host["mass"], host["ref_pos"],
                                          host["ref_vel"])
             rel = np.abs(pot[tidx] - phi_direct) / np.abs(phi_direct)
             p99[theta] = float(np.percentile(rel, 99))
+            ref = phi_reftree[k]
+            vs_tree = np.abs(pot[tidx] - ref) / np.abs(ref)
+            tree_err = np.abs(ref - phi_direct) / np.abs(phi_direct)
+            print(f"theta {theta}: vs reference tree p50 {np.median(vs_tree):.2e} "
+                  f"p99 {np.percentile(vs_tree, 99):.2e} max {vs_tree.max():.2e}; reference "
+                  f"tree vs direct sum p50 {np.median(tree_err):.2e} "
+                  f"p99 {np.percentile(tree_err, 99):.2e} max {tree_err.max():.2e}")
+            assert vs_tree.max() <= 1e-5, theta
             t0 = time.perf_counter()
             order, energy, res = ub.unbind(host)
             dt = time.perf_counter() - t0

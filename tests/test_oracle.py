@@ -42,6 +42,24 @@ def test_oracle_first_pass_golden(orc, case):
     assert nint > len(E)
 
 
+@pytest.mark.parametrize("case", FIRST_PASS_CASES)
+def test_oracle_tree_potentials_golden(orc, case):
+    """The targeted form (one tree, chosen targets, several opening angles) gives
+    the reference's first-pass potentials at the fixture's angle, and the full
+    first-pass walk's potentials at the others."""
+    par, inp, ref = load_case(case)
+    rng = np.random.default_rng(3)
+    t = np.sort(rng.choice(len(inp["mass"]), 300, replace=False))
+    thetas = (0.3, par["open_angle"], 0.7)
+    pot, cnt = orc.tree_potentials(par, inp["pos"], inp["mass"], t, thetas, nthreads=2)
+    np.testing.assert_array_equal(pot[1], ref["potential"][t])
+    for k in (0, 2):
+        _, full, _ = orc.binding_energies(dict(par, open_angle=thetas[k]), inp["pos"], inp["vel"],
+                                          inp["mass"], inp["ref_pos"], inp["ref_vel"], nthreads=1)
+        np.testing.assert_array_equal(pot[k], full[t])
+    assert cnt[0] > cnt[1] > cnt[2] > 0
+
+
 def test_oracle_batch_golden(orc):
     par, inp, ref = load_case("batch_48")
     order, energy, res = orc.unbind_batch(par, inp, nthreads=4)

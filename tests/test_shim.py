@@ -21,7 +21,9 @@ from helpers import load_case
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SHIM = os.path.join(ROOT, "tests", "shim")
 SO = os.path.join(SHIM, "_build", "libshim.so")
-REF_SRC = "/root/reference/src"
+from oracle import REFERENCE_DIR  # noqa: E402
+
+REF_SRC = os.path.join(REFERENCE_DIR, "src") if REFERENCE_DIR else ""
 
 
 def build_shim():
@@ -38,7 +40,7 @@ def test_shim_compiles():
     assert os.path.exists(build_shim())
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+@pytest.mark.skipif(not REF_SRC or not os.path.isdir(REF_SRC), reason="reference sources not present")
 def test_shim_compiles_against_reference_types(tmp_path):
     src = tmp_path / "use_ref.cpp"
     src.write_text('#include "subhalo.h"\n#include "hbtu_subhalo.hpp"\n'

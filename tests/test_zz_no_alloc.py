@@ -24,7 +24,7 @@ from helpers import load_case
 pytestmark = pytest.mark.gpu
 
 
-def _noalloc(lib, _lib, par, inp, torch):
+def _noalloc(lib, _lib, par, inp, torch, precision=0):
     """Run hbtu_unbind_noalloc on device copies of a subhalo; return host results."""
     from hbtplus_gb300.unbind import _state, params_from_dict
     n = len(inp["mass"])
@@ -38,7 +38,7 @@ def _noalloc(lib, _lib, par, inp, torch):
                             type=dev["type"].data_ptr(), location=_lib.HBTU_DEVICE, reserved=0)
     st = _state(inp["ref_pos"], inp["ref_vel"], inp["mostbound_pos"], inp["mostbound_vel"],
                 inp.get("mostbound_id", inp["id"][0]))
-    cp = params_from_dict(par)
+    cp = params_from_dict(par, precision=precision)
     stream = torch.cuda.current_stream().cuda_stream
     rc = lib.hbtu_unbind_noalloc(C.byref(cp), C.byref(p), n, C.byref(st), order.data_ptr(),
                                  energy.data_ptr(), res.data_ptr(), C.c_void_p(stream))
@@ -64,6 +64,42 @@ def test_noalloc_matches_unbind_on_two_calls_in_a_row():
         got = result_to_dict(r)
         for k, v in r_ref.items():
             np.testing.assert_array_equal(np.asarray(got[k]), np.asarray(v), err_msg=f"{case}: {k}")
+
+
+def _nfw(n, seed):
+    from hbtplus_gb300 import synthetic as S
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sub = S.nfw_subhalo(rng, n, 0.2 * (n / 1e5) ** (1 / 3), 10.0, contaminant_frac=0.2,
+                        center=rng.uniform(0, 100, 3))
+    S._assign_ids(rng, [sub])
+    return sub
+
+
+@pytest.mark.parametrize("precision,max_sample", [(0, 0), (1, 0), (0, 1000), (1, 1000)])
+def test_noalloc_multiblock_sizes_match_unbind(precision, max_sample):
+    """Subhaloes large enough for the multi-block sort (more than 4096 records:
+    its per-tile status words, tile counter and scan levels live in the scratch
+    array too), up to the stated capacity, in both walk precisions and with the
+    reference's sampled potentials; two calls in a row, each bit for bit equal
+    to hbtu_unbind."""
+    torch = pytest.importorskip("torch")
+    from hbtplus_gb300 import _lib
+    from hbtplus_gb300 import synthetic as S
+    from hbtplus_gb300.unbind import Unbinder, result_to_dict
+    lib = _lib.load()
+    par = S.default_params(max_sample_size=max_sample)
+    for n, seed in ((_lib.HBTU_NOALLOC_MAX_PARTICLES, 1), (9_000, 2)):
+        inp = _nfw(n, seed)
+        with Unbinder(par, precision=precision) as ub:
+            o_ref, e_ref, r_ref = ub.unbind(inp)
+        cp_par = dict(par)
+        order, energy, r = _noalloc(lib, _lib, cp_par, inp, torch, precision=precision)
+        tag = f"n={n} precision={precision} max_sample={max_sample}"
+        assert np.array_equal(order, o_ref), tag
+        assert np.array_equal(energy, e_ref, equal_nan=True), tag
+        got = result_to_dict(r)
+        for k, v in r_ref.items():
+            np.testing.assert_array_equal(np.asarray(got[k]), np.asarray(v), err_msg=f"{tag}: {k}")
 
 
 def test_noalloc_rejects_oversized_and_host_inputs():
