@@ -22,34 +22,30 @@
 //   warp: the warp visits the smallest index any of its targets waits at, so
 //     each node is a broadcast load (kept as an option for comparison).
 // FP64: absolute float coordinates, NEAREST per interaction, every operation
-// in the reference's order without fused multiply-add.
-#include "device_common.cuh"
+// in the reference's order without fused multiply-add; one walk per lane.
+// The per-target walks live in walk_ops.cuh (shared with small.cu).
+#include "walk_ops.cuh"
 
 namespace hbtu {
 namespace {
 
 constexpr int kWB = 128;
 
-struct Target {
-  int s, epos, pid, nxt, end;
-  bool active;
-  float q[3];  // position used by the walk (relative for FP32, absolute for FP64)
-  float mself;
-};
-
 // Target w of this pass: segment, list position, particle, walk range.
 template <bool kRel>
 __device__ __forceinline__ void load_target(const Ctx &c, int w, int total, Target &t)
 {
-  t.s = 0;
-  t.epos = -1;
-  t.pid = -1;
-  t.active = false;
-  t.nxt = kDone;
-  t.end = 0;
-  t.mself = 0.f;
-  t.q[0] = t.q[1] = t.q[2] = 0.f;
-  if (w >= total) return;
+  if (w >= total) {
+    t.s = 0;
+    t.epos = -1;
+    t.pid = -1;
+    t.active = false;
+    t.nxt = kDone;
+    t.end = 0;
+    t.mself = 0.f;
+    t.q[0] = t.q[1] = t.q[2] = 0.f;
+    return;
+  }
   const int k = upper_bound_i(c.tgt_base, c.S + 1, w) - 1;
   const int s = c.seg_order[k];
   const SegState &sg = c.seg[s];
@@ -71,136 +67,7 @@ __device__ __forceinline__ void load_target(const Ctx &c, int w, int total, Targ
     pid = c.epid[epos];
     active = true;
   }
-  t.s = s;
-  t.epos = epos;
-  t.pid = pid;
-  t.active = active;
-  if (!active) return;
-  const float4 a = c.pm[pid];
-  if (sg.mode != MODE_CORRECTION && epos - sg.off < sg.ntree) t.mself = fmul(a.w, sg.mfac);
-  if (kRel) {
-    t.q[0] = rel_coord(a.x, sg.fc[0], c.P);
-    t.q[1] = rel_coord(a.y, sg.fc[1], c.P);
-    t.q[2] = rel_coord(a.z, sg.fc[2], c.P);
-  } else {
-    t.q[0] = a.x;
-    t.q[1] = a.y;
-    t.q[2] = a.z;
-  }
-  const int root = 2 * c.tree_base[s];
-  const int nn = sg.ntree > 0 ? min(sg.nnodes, 2 * sg.ntree) : 0;  // node slots of this subhalo
-  t.end = root + nn;
-  t.nxt = nn > 0 ? root : kDone;
-}
-
-// BindingEnergy (full pass) or the correction update, and the store.
-__device__ __forceinline__ void finish_target(const Ctx &c, const Target &t, double pot_sum)
-{
-  if (!t.active) return;
-  const DevParams &P = c.P;
-  const SegState &sg = c.seg[t.s];
-  const double pot = ddiv(dmul(pot_sum, (double)P.G), (double)P.a);
-  const float4 a = c.pm[t.pid], v = c.vel[t.pid];
-  const float tp[3] = {a.x, a.y, a.z}, tv[3] = {v.x, v.y, v.z};
-  float E;
-  if (sg.mode != MODE_CORRECTION) {
-    float dv[3];
-    relvel(tp, tv, sg.ref_pos, sg.ref_vel, dv, P);
-    E = __double2float_rn(dadd(dmul((double)vdot(dv, dv), 0.5), pot));
-  } else {
-    float ov[3];
-    relvel(tp, tv, sg.old_pos, sg.old_vel, ov, P);
-    const float tt = fadd(vdot(ov, sg.dV), sg.dK);
-    E = __double2float_rn(dadd((double)c.eE[t.epos], dsub((double)tt, pot)));
-  }
-  if (sg.mode == MODE_REFINE)
-    c.eR[t.epos] = E;
-  else
-    c.eE[t.epos] = E;
-  if (c.pot_out) c.pot_out[t.epos] = pot;
-}
-
-__device__ __forceinline__ void count_interactions(const Ctx &c, int s, int n)
-{
-  const unsigned full = 0xffffffffu;
-  const int s0 = __shfl_sync(full, s, 0);
-  if (__all_sync(full, s == s0)) {
-    const int sum = __reduce_add_sync(full, n);
-    if ((threadIdx.x & 31) == 0 && sum)
-      atomicAdd((unsigned long long *)&c.seg[s0].interactions, (unsigned long long)sum);
-  } else if (n) {
-    atomicAdd((unsigned long long *)&c.seg[s].interactions, (unsigned long long)n);
-  }
-}
-
-// Opening test of the reference, len*len > r*r*theta^2: float first, and in
-// double with the reference's operation order when within 1e-5 of the edge.
-__device__ __forceinline__ bool opens(float4 na, const float q[3], float l2, float r2, float theta2,
-                                      double th2d)
-{
-  const float thr = r2 * theta2;
-  bool open = l2 > thr;
-  if (l2 > 0.f && fabsf(l2 - thr) <= 1e-5f * thr) {  // particles (l2 = 0) never open
-    const double ex = dsub((double)na.x, (double)q[0]);
-    const double ey = dsub((double)na.y, (double)q[1]);
-    const double ez = dsub((double)na.z, (double)q[2]);
-    const double er2 = dadd(dadd(dmul(ex, ex), dmul(ey, ey)), dmul(ez, ez));
-    open = (double)l2 > dmul(er2, th2d);
-  }
-  return open;
-}
-
-__device__ __forceinline__ float dist2(float4 na, const float q[3])
-{
-  const float dx = na.x - q[0], dy = na.y - q[1], dz = na.z - q[2];
-  return dx * dx + dy * dy + dz * dz;
-}
-
-// FP32 potential sum without double arithmetic in the walk loop (this GPU's
-// FP64 rate is 1/64 of its FP32 rate): interactions go into a short float
-// partial sum `f`, which is flushed every few steps into a compensated
-// (Kahan) float total hi - c.  The total is formed in double once per target.
-struct PotAcc {
-  float f = 0.f, hi = 0.f, c = 0.f;
-  __device__ __forceinline__ void flush()
-  {
-    const float y = __fsub_rn(f, c);
-    const float t = __fadd_rn(hi, y);
-    c = __fsub_rn(__fsub_rn(t, hi), y);
-    hi = t;
-    f = 0.f;
-  }
-  __device__ __forceinline__ double total(double base) const
-  {
-    return dadd(dadd(base, (double)hi), dsub((double)f, (double)c));
-  }
-};
-
-// Softened potential without a division: 1/u = h/r = h * rinv.
-__device__ __forceinline__ float softened_fp32(float m, float r2, float rinv, float hf, float hinvf)
-{
-  const float r = r2 * rinv;
-  const float u = r * hinvf;
-  float wp;
-  if (u < 0.5f)
-    wp = -2.8f + u * u * (5.333333333333f + u * u * (6.4f * u - 9.6f));
-  else
-    wp = -3.2f + 0.066666666667f * (hf * rinv) +
-         u * u * (10.666666666667f + u * (-16.0f + u * (9.6f - 2.133333333333f * u)));
-  return m * hinvf * wp;
-}
-
-// One monopole interaction in FP32: -m/r outside the softening length h,
-// the cubic-spline potential inside it (Springel, Yoshida & White 2001).
-__device__ __forceinline__ void interact(float4 na, float r2, float &pot_f, float hf, float h2f,
-                                         float hinvf)
-{
-  const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
-  const float m = fabsf(na.w);  // cells carry their mass with the sign bit set
-  if (r2 >= h2f)
-    pot_f = fmaf(-m, rinv, pot_f);
-  else
-    pot_f += softened_fp32(m, r2, rinv, hf, hinvf);
+  init_target<kRel>(c, s, epos, pid, active, 2 * c.tree_base[s], t);
 }
 
 // FP32 walk, warp schedule.  Leaf runs: when targets open a cell
@@ -291,83 +158,17 @@ __global__ void __launch_bounds__(kWB) k_walk_fp32(Ctx c, int total)
   count_interactions(c, t.s, ninter);
 }
 
-// The reference's opening decision in double, for a target whose float test
-// fell within 1e-5 of the threshold.  Not inlined: the compiler would
-// otherwise evaluate the double arithmetic on every step and select.
-// The target position comes by value, so the walk keeps it in registers.
-__device__ __noinline__ bool exact_open(float4 na, float qx, float qy, float qz, float l2,
-                                        double th2d)
-{
-  const double ex = dsub((double)na.x, (double)qx);
-  const double ey = dsub((double)na.y, (double)qy);
-  const double ez = dsub((double)na.z, (double)qz);
-  const double er2 = dadd(dadd(dmul(ex, ex), dmul(ey, ey)), dmul(ez, ez));
-  return (double)l2 > dmul(er2, th2d);
-}
-
-// FP32 walk, lane schedule: the opening test is two compares against
-// per-cell thresholds precomputed from len^2/theta^2 (the reference's double
-// test decides the rare cases in between), every interaction goes straight
-// into a compensated float sum, and the walk ends when the index leaves the
-// tree (skip pointers that leave it are kDone).
-//   kSib = false: preorder records; the next node is cur + 1 on opening, the
-//     skip pointer otherwise, so the index strictly grows and the loop ends
-//     even on a malformed tree.
-//   kSib = true: the sibling-block records (nd2): a cell's children sit in
-//     consecutive slots, so the sibling an accepted cell hands on to is
-//     usually in the same cache line; the next node is the first-child
-//     pointer (m.w) on opening and the skip pointer otherwise, the upper
-//     threshold is recomputed from the lower one, and the loop also stops
-//     after as many steps as the tree has nodes.  Same nodes, same order,
-//     same sums as the preorder walk.
-constexpr float kBandRatio = 1.0000200002f;  // (1 + 1e-5) / (1 - 1e-5), rounded up
-
+// FP32 walk, lane schedule (walk_lean): blocks of kB neighbouring targets.
 template <int kB, bool kSib>
 __global__ void __launch_bounds__(kB) k_walk_fp32_lean(Ctx c, int total)
 {
   HBTU_KERNEL_PROLOGUE();
-  const DevParams &P = c.P;
   Target t;
   load_target<true>(c, blockIdx.x * kB + threadIdx.x, total, t);
-  const float hf = (float)P.h, hinvf = (float)P.h_inv, h2f = hf * hf;
-  const double th2d = (double)P.theta2;
-  const WNode *nodes = kSib ? c.nd2 : c.nd;
-  float hi = 0.f, comp = 0.f;  // Kahan sum
-  int iters = 0, opens = 0;
-  int cur = t.nxt;
-  const int end = t.end;
-  const int steps = kSib ? max(end - t.nxt, 0) : 0;  // the tree's node count
-  while (cur < end) {
-    float4 na;
-    int4 nm;
-    load_node(nodes, cur, na, nm);
-    const float r2 = dist2(na, t.q);
-    const float lo = __int_as_float(nm.z);
-    const float up = kSib ? lo * kBandRatio : __int_as_float(nm.w);
-    bool open = r2 < lo;
-    if (r2 >= lo && r2 <= up)
-      open = exact_open(na, t.q[0], t.q[1], t.q[2], __int_as_float(nm.x & 0x7fffffff), th2d);
-    const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
-    const float mass = fabsf(na.w);
-    float contrib = -mass * rinv;
-    if (r2 < h2f) contrib = softened_fp32(mass, r2, rinv, hf, hinvf);
-    contrib = open ? 0.f : contrib;
-    const float y = __fsub_rn(contrib, comp);
-    const float s = __fadd_rn(hi, y);
-    comp = __fsub_rn(__fsub_rn(s, hi), y);
-    hi = s;
-    iters++;
-    opens += open ? 1 : 0;
-    if (kSib) {
-      cur = open ? nm.w : nm.y;
-      if (iters >= steps || cur < t.nxt) break;  // malformed pointers: stop
-    } else {
-      cur = open ? cur + 1 : max(nm.y, cur + 1);
-    }
-  }
-  const double base = (double)__fdiv_rn(t.mself, P.eps);  // cancels the self term
-  finish_target(c, t, dadd(dadd(base, (double)hi), -(double)comp));
-  count_interactions(c, t.s, iters - opens);
+  int ninter = 0;
+  const double pot = walk_lean<kSib>(kSib ? c.nd2 : c.nd, t, c.P, &ninter);
+  finish_target(c, t, pot);
+  count_interactions(c, t.s, ninter);
 }
 
 template <bool kSib>
@@ -381,58 +182,16 @@ void launch_lean(Ctx &c, int n)
     launch_k(k_walk_fp32_lean<128, kSib>, (n + 127) / 128, 128, 0, c.st, c, n);
 }
 
-// FP64: the reference's arithmetic, operation by operation.
+// FP64: the reference's arithmetic, operation by operation (walk_fp64), one
+// walk per lane.
 __global__ void __launch_bounds__(kWB) k_walk_fp64(Ctx c, int total)
 {
   HBTU_KERNEL_PROLOGUE();
-  const DevParams &P = c.P;
-  const unsigned full = 0xffffffffu;
   Target t;
   load_target<false>(c, blockIdx.x * kWB + threadIdx.x, total, t);
-  double pot_d = (double)__fdiv_rn(t.mself, P.eps);
-  const double th2d = (double)P.theta2;
   int ninter = 0;
-  int cur = __reduce_min_sync(full, t.nxt);
-  while (cur != kDone) {
-    const float4 na = c.nd_abs[cur];
-    const int2 nm = make_int2(c.nd[cur].m.x, c.nd[cur].m.y);
-    if (t.nxt == cur) {
-      double dx = dsub((double)na.x, (double)t.q[0]);
-      double dy = dsub((double)na.y, (double)t.q[1]);
-      double dz = dsub((double)na.z, (double)t.q[2]);
-      if (P.periodic) {
-        dx = nearest_d(dx, P);
-        dy = nearest_d(dy, P);
-        dz = nearest_d(dz, P);
-      }
-      const double r2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
-      if ((double)__int_as_float(nm.x & 0x7fffffff) > dmul(r2, th2d)) {
-        t.nxt = cur + 1 < t.end ? cur + 1 : kDone;
-      } else {
-        const int sk = nm.y;
-        t.nxt = (unsigned)(sk - cur - 1) < (unsigned)(t.end - cur - 1) ? sk : kDone;
-        ninter++;
-        const double mass = (double)na.w;
-        const double r = __dsqrt_rn(r2);
-        if (r >= P.h) {
-          pot_d = dsub(pot_d, ddiv(mass, r));
-        } else {
-          const double u = dmul(r, P.h_inv);
-          const double uu = dmul(u, u);
-          double wp;
-          if (u < 0.5)
-            wp = dadd(-2.8, dmul(uu, dadd(5.333333333333, dmul(uu, dsub(dmul(6.4, u), 9.6)))));
-          else
-            wp = dadd(dadd(-3.2, ddiv(0.066666666667, u)),
-                      dmul(uu, dadd(10.666666666667,
-                                    dmul(u, dadd(-16.0, dmul(u, dsub(9.6, dmul(2.133333333333, u))))))));
-          pot_d = dadd(pot_d, dmul(dmul(mass, P.h_inv), wp));
-        }
-      }
-    }
-    cur = __reduce_min_sync(full, t.nxt);
-  }
-  finish_target(c, t, pot_d);
+  const double pot = walk_fp64(c, t, &ninter);
+  finish_target(c, t, pot);
   count_interactions(c, t.s, ninter);
 }
 

@@ -16,8 +16,12 @@ Tolerances:
   FP32 mode: a particle may change side only if its energy lies in the band
     |E| <= 1e-5 * max|E_bound|; Mbound within 1e-5 relative plus one particle
     mass per changed particle; bound energies within 2e-6 * max|E_bound|
-    (subhaloes where no particle changed side); iteration and interaction
-    counts exact; the same most-bound particle unless the reference's two
+    (subhaloes where no particle changed side); iteration counts exact;
+    interaction counts within 1e-6 relative (the walk takes the reference's
+    opening decision in double near the threshold, but on float coordinates
+    relative to the frame, which are exact except across a periodic face when
+    one side lies close to 0: a decision within ~1e-7 of the threshold can
+    then flip); the same most-bound particle unless the reference's two
     lowest energies lie within 2e-6 * max|E_bound| of each other.
   FP64 mode: Nbound, Mbound, iterations, frames and bound energies bit for
     bit, the order up to runs of equal energy.  Cells below
@@ -76,7 +80,13 @@ def refined_energies(orc, p, b, a, orf, nbr, r, max_sample):
     return e
 
 
-def compare(batch, got, ref, exact, orc=None, p=None):
+def straddles(batch, a, b):
+    """True if the subhalo's particles lie on both sides of a periodic face."""
+    x = np.asarray(batch["pos"][a:b], np.float64)
+    return bool(np.any(x.max(axis=0) - x.min(axis=0) > 50.0))
+
+
+def compare(batch, got, ref, exact, orc=None, p=None, counts=None):
     """Per-subhalo comparison; returns (changed side, inexact subhaloes)."""
     max_sample = int(p["max_sample_size"]) if p else 0
     order, energy, res = got
@@ -84,6 +94,8 @@ def compare(batch, got, ref, exact, orc=None, p=None):
     off = batch["offsets"]
     changed = 0
     inexact = 0
+    if counts is not None:
+        counts.clear()
     for s in range(len(off) - 1):
         a, b = int(off[s]), int(off[s + 1])
         n = b - a
@@ -116,7 +128,11 @@ def compare(batch, got, ref, exact, orc=None, p=None):
                 assert np.max(np.abs(eg[:nb] - erf[:nb])) <= BAND * emax, tag
                 assert abs(g["interactions"] - r["interactions"]) <= 1e-5 * r["interactions"], tag
             continue
-        assert g["interactions"] == r["interactions"], tag
+        if g["interactions"] != r["interactions"]:
+            assert abs(g["interactions"] - r["interactions"]) <= 1e-6 * r["interactions"], tag
+            if counts is not None:
+                counts.append((s, n, int(g["interactions"] - r["interactions"]),
+                               straddles(batch, a, b)))
         mg = np.zeros(n, bool)
         mr = np.zeros(n, bool)
         mg[og[:nb]] = True
@@ -157,11 +173,15 @@ def test_full_batch_against_oracle(batch, orc, max_sample):
     for precision in (0, 1):
         with Unbinder(p, precision=precision) as ub:
             got = ub.unbind_batch(b)
-        changed, inexact = compare(b, got, ref, exact=precision == 1, orc=orc, p=p)
+        counts = []
+        changed, inexact = compare(b, got, ref, exact=precision == 1, orc=orc, p=p,
+                                   counts=counts)
         nbound = sum(int(r["nbound"]) for r in got[2])
         print(f"max_sample {max_sample} precision {'fp64' if precision else 'fp32'}: "
               f"nbound {nbound}, {changed} particles changed side (all inside the band), "
-              f"{inexact} subhaloes with sub-resolution cells not bit-exact")
+              f"{inexact} subhaloes with sub-resolution cells not bit-exact, "
+              f"interaction counts not exact in {len(counts)} subhaloes "
+              f"(subhalo, n, difference, straddles a face): {counts[:10]}")
         if precision == 1:
             assert inexact <= 20  # of 2000
         # size-independent properties of the outputs
