@@ -76,6 +76,12 @@ def parse():
                     help="walk_layout option of the FP32 walk (-1: library default)")
     ap.add_argument("--walk-schedule", type=int, default=-1,
                     help="walk_schedule option of the FP32 walk (-1: library default)")
+    ap.add_argument("--small-cutoff", type=int, default=-1,
+                    help="small_cutoff option: once every active subhalo's list is at most "
+                         "this long, one block per subhalo finishes the loop (-1: library "
+                         "default, 0: off)")
+    ap.add_argument("--small-blocks", type=int, default=-1,
+                    help="small_blocks_per_sm option (-1: library default)")
 
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -458,6 +464,12 @@ def main():
         ub.set_option("walk_schedule", args.walk_schedule)
     if args.walk_layout >= 0:
         ub.set_option("walk_layout", args.walk_layout)
+    if args.small_cutoff >= 0:
+        ub.set_option("small_cutoff", args.small_cutoff)
+    if args.small_blocks >= 0:
+        ub.set_option("small_blocks_per_sm", args.small_blocks)
+    small_cutoff = ub.get_option("small_cutoff")
+    small_blocks = ub.get_option("small_blocks_per_sm")
 
     stream = torch.cuda.current_stream(dev)
     ub.set_stream(stream.cuda_stream)
@@ -663,10 +675,14 @@ def main():
         "plain": plain,
         "batched_over_plain": (value / ws) / plain["value"] if plain else None,
         "accuracy_vs_cpu_reference": accuracy,
-        "phase_ms_per_step": {"tree": st["tree_ms"] / args.steps, "walk": walk_ms,
+        "phase_ms_per_step": {"small": st["small_ms"] / args.steps,
+                              "tree": st["tree_ms"] / args.steps, "walk": walk_ms,
                               "loop": st["loop_ms"] / args.steps,
-                              "passes": st["passes"] / args.steps},
+                              "passes": st["passes"] / args.steps,
+                              "small_subhaloes": st["small_subhaloes"] / args.steps},
     }
+    line["config"]["small_cutoff"] = small_cutoff
+    line["config"]["small_blocks_per_sm"] = small_blocks
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -92,6 +92,7 @@ class hbtu_stats(C.Structure):
         ("kernel_launches", C.c_int64), ("walk_launches", C.c_int64),
         ("evaluations", C.c_int64), ("interactions", C.c_int64),
         ("walk1_ms", C.c_double), ("walk1_interactions", C.c_int64),
+        ("small_ms", C.c_double), ("small_subhaloes", C.c_int64),
     ]
 
 

@@ -18,8 +18,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libhbtu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["prims.cu", "tree.cu", "walk.cu", "loop.cu", "capi.cu", "noalloc.cu", "direct.cu",
-           "index.cu", "props.cu", "merge.cu"]
+SOURCES = ["prims.cu", "tree.cu", "walk.cu", "loop.cu", "small.cu", "capi.cu", "noalloc.cu",
+           "direct.cu", "index.cu", "props.cu", "merge.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
                      "-I" + INCLUDE]

@@ -62,6 +62,7 @@ static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S, boo
   c.plan_cnt = cv.take<int4>(S);
   c.plan_cnt2 = cv.take<int4>(S);
   c.plan_inter = cv.take<long long>(S);
+  c.small_next = cv.take<int>(1);
   c.part_info = cv.take<int>(8 * S);
   c.chunk_bbox = cv.take<unsigned>(6 * maxchunks);
   c.chunk_sums = cv.take<double>(24 * maxchunks);
@@ -259,6 +260,10 @@ hbtu_status setup_call(hbtu_handle *h, const hbtu_particles *p, long long S, con
   for (long long s = 0; s < S; s++) order[s] = (int)s;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return segs[a].n > segs[b].n; });
+  // the per-subhalo loop takes over small subhaloes (small.cu); the walk of
+  // its blocks is the default one-target-per-lane schedule
+  c.small_cap = h->opt_schedule == 0 ? (int)std::min<int64_t>(h->opt_small, kSmallCap) : 0;
+  c.small_per_sm = (int)h->opt_small_per_sm;
   if (S > 0) {
     HBTU_CUDA(cudaMemcpyAsync(c.seg, segs.data(), sizeof(SegState) * S, cudaMemcpyHostToDevice,
                               c.st));
@@ -298,10 +303,30 @@ struct PhaseTimer : LoopHooks {
     HBTU_CUDA(cudaEventRecord(event_at(h, next), st));
     marks.push_back(next++);
   }
+  // the per-subhalo loop of the small subhaloes (its own pair of events)
+  int small_ev[2] = {-1, -1};
+  void small_begin() override
+  {
+    if (!h->timing) return;
+    HBTU_CUDA(cudaEventRecord(event_at(h, next), st));
+    small_ev[0] = (int)next++;
+  }
+  void small_end() override
+  {
+    if (!h->timing) return;
+    HBTU_CUDA(cudaEventRecord(event_at(h, next), st));
+    small_ev[1] = (int)next++;
+  }
   // marks come in groups of 4: before tree, after tree, after walk, after loop
   int group = 0;  // pass groups collected in this call
   void collect() override
   {
+    if (small_ev[0] >= 0 && small_ev[1] >= 0) {
+      float ms = 0.f;
+      HBTU_CUDA(cudaEventElapsedTime(&ms, h->events[small_ev[0]], h->events[small_ev[1]]));
+      h->stats.small_ms += ms;
+      small_ev[0] = small_ev[1] = -1;
+    }
     for (size_t i = 0; i + 3 < marks.size(); i += 4) {
       float a = 0, b = 0, c = 0;
       HBTU_CUDA(cudaEventElapsedTime(&a, h->events[marks[i]], h->events[marks[i + 1]]));
@@ -384,6 +409,15 @@ void run_passes(Ctx &c, int max_passes, LoopHooks *hk)
     if (pass == 1 && hk && hk->stats) hk->stats->walk1_interactions += pl.inter_done;
     launch_block_sort(c, pl.nsort_total, 0);  // unbound blocks of the previous pass
     if (pl.nactive == 0) break;
+    if (pl.max_nlast <= c.small_cap) {
+      // every active subhalo is small: one block per subhalo runs its
+      // remaining passes to the end (small.cu), and the loop is done
+      if (hk) hk->small_begin();
+      launch_small(c, c.small_cap, pl.nactive, max_passes);
+      if (hk) hk->small_end();
+      if (hk && hk->stats) hk->stats->small_subhaloes += pl.nactive;
+      break;
+    }
     if (hk && hk->stats) hk->stats->passes++;
     pass_tree_and_energies(c, hk);
     launch_partition(c);
@@ -392,6 +426,7 @@ void run_passes(Ctx &c, int max_passes, LoopHooks *hk)
   }
   launch_plan(c, 2);
   read_plan(c);
+  if (hk) hk->collect();
   const int nrefine = c.plan_host->nrefine;
   launch_block_sort(c, c.plan_host->nsort_total, 1);  // bound blocks (:405)
   if (nrefine > 0) {  // RefineBindingEnergyOrder (:406-407)
@@ -439,7 +474,7 @@ using namespace hbtu;
 
 extern "C" {
 
-int32_t hbtu_version(void) { return 10000; }
+int32_t hbtu_version(void) { return 10100; }
 
 const char *hbtu_last_error(const hbtu_handle *h)
 {
@@ -532,6 +567,19 @@ hbtu_status hbtu_set_option(hbtu_handle *h, const char *name, int64_t value)
     h->opt_layout = value;
     return HBTU_OK;
   }
+  if (n == "small_cutoff") {
+    if (value < 0 || value > kSmallCap)
+      return fail(h, HBTU_ERR_INVALID_ARGUMENT,
+                  "small_cutoff: 0 (off) to " + std::to_string(kSmallCap));
+    h->opt_small = value;
+    return HBTU_OK;
+  }
+  if (n == "small_blocks_per_sm") {
+    if (value < 1 || value > 8)
+      return fail(h, HBTU_ERR_INVALID_ARGUMENT, "small_blocks_per_sm: 1 to 8");
+    h->opt_small_per_sm = value;
+    return HBTU_OK;
+  }
   return fail(h, HBTU_ERR_INVALID_ARGUMENT, "unknown option " + n);
 }
 
@@ -549,6 +597,14 @@ hbtu_status hbtu_get_option(const hbtu_handle *h, const char *name, int64_t *val
   }
   if (n == "walk_layout") {
     *value = h->opt_layout;
+    return HBTU_OK;
+  }
+  if (n == "small_cutoff") {
+    *value = h->opt_small;
+    return HBTU_OK;
+  }
+  if (n == "small_blocks_per_sm") {
+    *value = h->opt_small_per_sm;
     return HBTU_OK;
   }
   return HBTU_ERR_INVALID_ARGUMENT;

@@ -188,6 +188,11 @@ struct Ctx {
   // adjoint outputs (hbtu_energy_gradient), by input position; grads may be null
   float *grad_pos, *grad_vel, *grad_mass;
   double *e_part;
+  // the per-subhalo loop (small.cu): it takes over once every active
+  // subhalo's list holds at most small_cap particles (0: never)
+  int *small_next;   // work-queue counter
+  int small_cap;
+  int small_per_sm;  // blocks per SM of its persistent launch
 };
 
 // launchers (tree.cu)
@@ -212,6 +217,12 @@ void launch_segment_sums(Ctx &c, const double *x, double *out);
 // (direct.cu) exact FP64 potentials of particles tidx[0..nt) from all n particles
 void direct_potential_fp64(const DevParams &P, const float4 *pm, int n, const int *tidx, int nt,
                            double *out, double *partial, int nsplit, cudaStream_t st);
+// (small.cu) the remaining passes of every active subhalo, one block per
+// subhalo; `cap` bounds their energy lists (at most kSmallCap particles)
+constexpr int kSmallCap = 2048;
+constexpr int kSmallDefault = 2048;
+void launch_small(Ctx &c, int cap, int nactive, int max_passes);
+size_t small_smem_bytes(int cap);
 // launchers (loop.cu)
 void launch_init(Ctx &c, const float *pos, const float *vel, const float *mass,
                  const long long *id);

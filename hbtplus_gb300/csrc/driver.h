@@ -33,6 +33,8 @@ struct LoopHooks {
   hbtu_stats *stats = nullptr;
   virtual void mark() {}
   virtual void collect() {}
+  virtual void small_begin() {}
+  virtual void small_end() {}
   virtual ~LoopHooks() {}
 };
 

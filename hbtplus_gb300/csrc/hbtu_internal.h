@@ -93,6 +93,7 @@ struct PassPlan {
   int nchunks_bound;
   int nrefine;
   int error;             // a sort's look-back wait ran out
+  int max_nlast;         // longest energy list of an active subhalo
   long long inter_done;  // walk interactions summed so far, all subhaloes
 };
 

@@ -184,6 +184,7 @@ __global__ void k_plan_gather(Ctx c, int mode)
     c.plan_cnt[s] = counts_of<get_pass>(c, s);
     int4 t = counts_of<get_targets_sorted>(c, s);  // by position in size order
     t.y = c.seg[s].status == SEG_ACTIVE;           // summed only
+    t.z = t.y ? c.seg[s].nlast : 0;                // maximum only
     c.plan_cnt2[s] = t;
     c.plan_inter[s] = c.seg[s].interactions;
   } else if (mode == 1) {
@@ -225,25 +226,37 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode, int gath
     __shared__ unsigned long long inter;
     if (threadIdx.x == 0) inter = 0;
     __syncthreads();
-    int cnt = 0;
+    __shared__ int maxn;
+    if (threadIdx.x == 0) maxn = 0;
+    __syncthreads();
+    int cnt = 0, mx = 0;
     unsigned long long it = 0;
     for (int s = threadIdx.x; s < c.S; s += kPlanThreads) {
       if (gathered) {
         it += (unsigned long long)c.plan_inter[s];
+        mx = max(mx, c.plan_cnt2[s].z);
       } else {
-        cnt += c.seg[s].status == SEG_ACTIVE;
-        it += (unsigned long long)c.seg[s].interactions;
+        const SegState &sg = c.seg[s];
+        const bool act = sg.status == SEG_ACTIVE;
+        cnt += act;
+        mx = max(mx, act ? sg.nlast : 0);
+        it += (unsigned long long)sg.interactions;
       }
     }
     // warp sums first: one shared atomic per warp, not per thread
     cnt = __reduce_add_sync(0xffffffffu, cnt);
+    mx = __reduce_max_sync(0xffffffffu, mx);
     for (int o = 16; o > 0; o >>= 1) it += __shfl_xor_sync(0xffffffffu, it, o);
     if ((threadIdx.x & 31) == 0) {
       atomicAdd(&nact, cnt);
       atomicAdd(&inter, it);
+      atomicMax(&maxn, mx);
     }
     __syncthreads();
-    if (threadIdx.x == 0) c.plan->inter_done = (long long)inter;
+    if (threadIdx.x == 0) {
+      c.plan->inter_done = (long long)inter;
+      c.plan->max_nlast = maxn;
+    }
     if (gathered)
       plan_scan4<get_cnt>(c.S, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
     else

@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kTB) k_leaves(Ctx c, int ntotal)
   if (e >= ntotal) return;
   const int s = c.sb.hi_a[e];
   const int base = c.tree_base[s], n = c.tree_base[s + 1] - base;
-  leaves_elem(c, c.seg[s], base, n, e, c.pm[c.epid[c.sb.val_a[e]]], c.sb.lo_a[e]);
+  leaves_elem(c, c.seg[s], base, n, e, c.pm[c.epid[c.sb.val_a[e]]], c.sb.lo_a[e], c.X + base);
 }
 
 __global__ void __launch_bounds__(kTB) k_cellnodes(Ctx c, int ntotal)
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(kTB) k_cellnodes(Ctx c, int ntotal)
   }
   const int s = c.sb.hi_a[e];
   const int base = c.tree_base[s], n = c.tree_base[s + 1] - base;
-  cellnodes_elem(c, c.seg[s], base, n, e, c.sb.lo_a + base);
+  cellnodes_elem(c, c.seg[s], base, n, e, c.sb.lo_a + base, c.X + base);
 }
 
 // Bottom-up moments (cell_moment): a cell is summed once all its child cells

@@ -261,10 +261,13 @@ __device__ __forceinline__ float4 make_rel(float4 a, const float fc[3], const De
 
 // Particle leaf j of a subhalo's tree (element e = base + j): preorder index
 // j + #cells starting at or before key j; a0 is its particle {x, y, z, m}
-// (mass not yet scaled by the sampling factor).  The subhalo of one particle
-// gets a root cell of side 0 holding it (tpp:56-102 with one particle).
+// (mass not yet scaled by the sampling factor).  Xs[0..n]: the exclusive scan
+// of the cells starting at each of the subhalo's keys (any common offset).
+// The subhalo of one particle gets a root cell of side 0 holding it
+// (tpp:56-102 with one particle).
 __device__ __forceinline__ void leaves_elem(const Ctx &c, SegState &sg, int base, int n, int e,
-                                            float4 a0, unsigned long long key)
+                                            float4 a0, unsigned long long key,
+                                            const long long *Xs)
 {
   const int j = e - base;
   const int nb = 2 * base;
@@ -280,9 +283,9 @@ __device__ __forceinline__ void leaves_elem(const Ctx &c, SegState &sg, int base
     sg.nnodes = 2;
     return;
   }
-  const long long xb = c.X[base];
-  const int idx = j + (int)(c.X[e + 1] - xb);
-  const int nnodes = n + (int)(c.X[base + n] - xb);
+  const long long xb = Xs[0];
+  const int idx = j + (int)(Xs[j + 1] - xb);
+  const int nnodes = n + (int)(Xs[n] - xb);
   c.nd_abs[nb + idx] = a;
   c.nd[nb + idx].p = make_rel(a, sg.fc, c.P);
   c.nd[nb + idx].m = particle_meta(idx + 1 < nnodes ? nb + idx + 1 : kDone);
@@ -298,18 +301,20 @@ __device__ __forceinline__ void leaves_elem(const Ctx &c, SegState &sg, int base
 
 // Cell e (an internal node with iscell[e] set): preorder index, skip pointer,
 // side (len*len in float), octal depth, and a count of child cells on the
-// parent.  keys: the subhalo's sorted keys, element-indexed from `base`.
+// parent.  keys: the subhalo's sorted keys, element-indexed from `base`; Xs
+// as for leaves_elem.
 __device__ __forceinline__ void cellnodes_elem(const Ctx &c, const SegState &sg, int base, int n,
-                                               int e, const unsigned long long *keys)
+                                               int e, const unsigned long long *keys,
+                                               const long long *Xs)
 {
   const int nb = 2 * base;
   const int od = oct_depth(c.dnode[e], sg.levels);
   const int lo = c.rfirst[e], hi = c.rlast[e];
   const unsigned long long m = c.mask[base + lo];
   const int rank = __popcll(m & ((1ull << od) - 1ull));
-  const long long xb = c.X[base];
-  const int idx = lo + (int)(c.X[base + lo] - xb) + rank;
-  const int skip = hi + 1 + (int)(c.X[base + hi + 1] - xb);
+  const long long xb = Xs[0];
+  const int idx = lo + (int)(Xs[lo] - xb) + rank;
+  const int skip = hi + 1 + (int)(Xs[hi + 1] - xb);
   double len = sg.len;
   for (int k = 0; k < od; k++)
     if (len >= (double)c.P.res) len = dmul(len, 0.5);

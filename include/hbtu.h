@@ -198,6 +198,8 @@ typedef struct hbtu_stats {
   int64_t interactions;    /* tree-walk contributions summed */
   double walk1_ms;         /* with timing on: the first pass's walk of each call */
   int64_t walk1_interactions; /* contributions summed by those first-pass walks */
+  double small_ms;         /* with timing on: the per-subhalo loop (option "small_cutoff") */
+  int64_t small_subhaloes; /* subhaloes whose last passes ran in it */
 } hbtu_stats;
 
 /* Turn per-phase device timing on (1) or off (0; the default).  With timing
@@ -207,6 +209,15 @@ hbtu_status hbtu_get_stats(const hbtu_handle *h, hbtu_stats *out);
 hbtu_status hbtu_reset_stats(hbtu_handle *h);
 
 /* Tuning options of a handle (results do not depend on them):
+ *   "small_cutoff"    (default 2048, at most 2048; 0: off) from the first
+ *                     round of the loop at which every active subhalo's
+ *                     energy list holds at most this many particles, one
+ *                     persistent launch finishes them all, one thread block
+ *                     per subhalo running its remaining passes (a work queue
+ *                     in size order); before it, every active subhalo
+ *                     advances one pass per round of batch kernels.  With
+ *                     walk_schedule 1 it is off.
+ *   "small_blocks_per_sm" (default 1, 1..8) blocks per SM of that launch.
  *   "walk_schedule"   how the FP32 walk visits nodes: 0 (default) every
  *                     lane walks its own target; 1 a warp visits the smallest
  *                     node index any of its targets waits at (broadcast loads).

@@ -37,8 +37,9 @@ def test_struct_layouts_match_header():
 #include "hbtu.h"
 #define P(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
 int main(void) {
-  printf("params %zu\nstate %zu\nresult %zu\nparticles %zu\n", sizeof(hbtu_params),
-         sizeof(hbtu_state), sizeof(hbtu_result), sizeof(hbtu_particles));
+  printf("params %zu\nstate %zu\nresult %zu\nparticles %zu\nstats %zu\n", sizeof(hbtu_params),
+         sizeof(hbtu_state), sizeof(hbtu_result), sizeof(hbtu_particles), sizeof(hbtu_stats));
+  P(hbtu_stats, small_ms) P(hbtu_stats, small_subhaloes)
   P(hbtu_result, nbound_type) P(hbtu_result, iterations) P(hbtu_result, evaluations)
   P(hbtu_result, status) P(hbtu_params, precision) P(hbtu_params, device)
   P(hbtu_state, mostbound_id) P(hbtu_particles, location)
@@ -56,6 +57,7 @@ int main(void) {
     assert int(got["state"]) == C.sizeof(_lib.hbtu_state)
     assert int(got["result"]) == C.sizeof(_lib.hbtu_result)
     assert int(got["particles"]) == C.sizeof(_lib.hbtu_particles)
+    assert int(got["stats"]) == C.sizeof(_lib.hbtu_stats)
     for key, val in got.items():
         if "." in key:
             t, f = key.split(".")

@@ -67,11 +67,15 @@ def test_noalloc_matches_unbind_on_two_calls_in_a_row():
 
 
 def _nfw(n, seed):
+    """An NFW subhalo with contaminants, cut to exactly n particles."""
     from hbtplus_gb300 import synthetic as S
     rng = np.random.Generator(np.random.PCG64(seed))
     sub = S.nfw_subhalo(rng, n, 0.2 * (n / 1e5) ** (1 / 3), 10.0, contaminant_frac=0.2,
                         center=rng.uniform(0, 100, 3))
     S._assign_ids(rng, [sub])
+    for k in ("id", "pos", "vel", "mass", "type"):
+        sub[k] = np.ascontiguousarray(sub[k][:n])
+    assert len(sub["mass"]) == n
     return sub
 
 
