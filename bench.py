@@ -17,7 +17,10 @@ softening 0.002 Mpc/h, opening angle 0.45.
   cpu_baseline  the reference CPU path on the same batch on this host's cores
 
 python bench.py [--steps K] [--warmup W] [--impl reference]; under torchrun
-every rank unbinds its own batch (independent subhaloes: weak scaling).
+the job is one global batch split across the ranks by the planner of
+hbtplus_gb300.shard (greedy LPT on n log n; no device collective, the results
+are gathered on the host afterwards): by default N copies of the workload with
+different seeds (weak scaling), with --scaling strong one workload split N ways.
 """
 from __future__ import annotations
 
@@ -59,12 +62,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nsub", type=int, default=2000)
-    ap.add_argument("--workload", default="batch", choices=["batch", "single", "host2e7", "step"],
+    ap.add_argument("--workload", default="batch",
+                    choices=["batch", "single", "host2e7", "step", "adjoint"],
                     help="batch: the 2000-subhalo batch (default); single: the isolated "
                          "1e5-particle NFW subhalo (+10%% contaminants); host2e7: the "
                          "2e7-particle host with 300 clumps (+5%% contaminants); step: a "
                          "tracking step of 20,000 subhaloes in a 3e7-particle snapshot (ID "
-                         "re-resolve, gather, unbind)")
+                         "re-resolve, gather, unbind); adjoint: the batched backward of the "
+                         "2000-subhalo batch's bound sets (one hbtu_energy_gradient call)")
     ap.add_argument("--open-angle", type=float, default=0.45)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--leaf-runs", type=int, default=-1,
@@ -82,7 +87,10 @@ def parse():
                          "default, 0: off)")
     ap.add_argument("--small-blocks", type=int, default=-1,
                     help="small_blocks_per_sm option (-1: library default)")
-
+    ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
+                    help="under torchrun: weak (default) -- a global batch of N workloads, "
+                         "one per rank's worth, split across the ranks by the LPT planner; "
+                         "strong -- one workload split N ways")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -105,6 +113,21 @@ def workload(nsub: int, rank: int, kind: str = "batch", theta: float = 0.45,
         return S.concat([S.host_with_clumps(seed=20261205 + 1000 * rank)]), p
     b = S.subhalo_batch(nsub=nsub, seed=20261204 + 1000 * rank)
     return b, p
+
+
+def global_workload(args, ws):
+    """The whole job's batch: ws workloads (seeds per rank) concatenated for weak
+    scaling, one workload for strong scaling; every rank builds the same."""
+    from hbtplus_gb300 import synthetic as S
+    copies = ws if args.scaling == "weak" else 1
+    parts, params = [], None
+    for r in range(copies):
+        b, params = workload(args.nsub, r, args.workload, args.open_angle, args.max_sample)
+        parts.append(b)
+    if copies == 1:
+        return parts[0], params
+    subs = [S.split(b, s) for b in parts for s in range(len(b["offsets"]) - 1)]
+    return S.concat(subs), params
 
 
 def cpu_threads() -> int:
@@ -237,7 +260,7 @@ def copy_times(pin, dev, outs, stream, steps):
 def run_reference_arm(args, ws, rank):
     if rank != 0:
         return
-    if args.workload in ("step", "host2e7"):
+    if args.workload in ("step", "host2e7", "adjoint"):
         print(json.dumps({"impl": "reference", "unavailable":
                           f"the {args.workload} workload has no CPU reference run: one pass "
                           "of the reference over it takes minutes on the host"}), flush=True)
@@ -428,6 +451,105 @@ def run_tracking_step(args, ws, rank, local):
     ub.close()
 
 
+def run_adjoint(args, ws, rank, local):
+    """The batched backward of config 3: the 2000-subhalo batch is unbound, and
+    the binding energies of all its bound sets are differentiated with respect
+    to positions, velocities and masses in one hbtu_energy_gradient call."""
+    import torch
+
+    from hbtplus_gb300 import _lib
+    from hbtplus_gb300.adjoint import bound_subset, energy_gradient
+    from hbtplus_gb300.unbind import Unbinder, _state
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    batch, params = workload(args.nsub, rank, "batch", args.open_angle, 0)
+    ub = Unbinder(params, device=local)
+    order, _, res = ub.unbind_batch(batch)
+    b = bound_subset(batch, order, res)
+    nsub = len(b["offsets"]) - 1
+    npart = int(b["offsets"][-1])
+    T = {k: torch.from_numpy(b[k]).to(dev) for k in ("pos", "vel", "mass")}
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def step():
+        return energy_gradient(ub, T["pos"], T["vel"], T["mass"], b["offsets"], b["ref_pos"],
+                               b["ref_vel"])
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ub.reset_stats()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            times.append((e0, e1))
+        torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(c) for a, c in times) / args.steps
+    launches = int(ub.stats()["kernel_launches"]) // max(1, args.steps)
+    # end to end: host arrays through the C ABI, gradients back to the host
+    pin = {k: torch.from_numpy(b[k]).pin_memory() for k in ("pos", "vel", "mass")}
+    ids = torch.arange(npart, dtype=torch.int64).pin_memory()
+    gp = torch.empty((npart, 3), dtype=torch.float32).pin_memory()
+    gv = torch.empty((npart, 3), dtype=torch.float32).pin_memory()
+    gm = torch.empty(npart, dtype=torch.float32).pin_memory()
+    E = np.zeros(nsub, np.float64)
+    off = np.ascontiguousarray(b["offsets"], np.int64)
+    sts = (_lib.hbtu_state * nsub)()
+    for s in range(nsub):
+        sts[s] = _state(b["ref_pos"][s], b["ref_vel"][s], b["ref_pos"][s], b["ref_vel"][s], -1)
+    p_host = _lib.hbtu_particles(id=ids.data_ptr(), pos=pin["pos"].data_ptr(),
+                                 vel=pin["vel"].data_ptr(), mass=pin["mass"].data_ptr(), type=0,
+                                 location=_lib.HBTU_HOST, reserved=0)
+
+    def e2e_step():
+        rc = ub.lib.hbtu_energy_gradient(ub.handle, C.byref(p_host), nsub, off.ctypes.data,
+                                         C.addressof(sts), E.ctypes.data, gp.data_ptr(),
+                                         gv.data_ptr(), gm.data_ptr())
+        _lib.check(rc, ub.handle)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_t) / args.steps
+    h2d = npart * (12 + 12 + 4 + 8) + off.nbytes + C.sizeof(sts)
+    d2h = npart * (12 + 12 + 4) + nsub * 8
+    line = {
+        "metric": "subhalo binding-energy gradients/s (batched backward of the bound sets)",
+        "value": ws * nsub / (ms / 1e3), "unit": "subhalo gradients/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (the 2000-subhalo batch, unbound; its bound sets)",
+        "config": {"workload": "adjoint: d E_tot / d(x, v, m) of the bound sets of the "
+                               "2000-subhalo batch in one call", "nsub": nsub,
+                   "bound_particles": npart, "open_angle": args.open_angle,
+                   "l2": "flushed before each timed step (256 MB write)"},
+        "particles_per_s": ws * npart / (ms / 1e3),
+        "e2e": {"value": ws * nsub / e2e_s, "unit": "subhalo gradients/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s},
+        "gpu_launches": launches,
+        "cpu_baseline": None,
+        "cpu_baseline_note": "the reference has no adjoint",
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ub.close()
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
@@ -440,8 +562,8 @@ def main():
             import torch.distributed as dist
             dist.destroy_process_group()
         return
-    if args.workload == "step":
-        run_tracking_step(args, ws, rank, local)
+    if args.workload in ("step", "adjoint"):
+        (run_tracking_step if args.workload == "step" else run_adjoint)(args, ws, rank, local)
         if ws > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
@@ -451,9 +573,15 @@ def main():
     from hbtplus_gb300 import _lib
     from hbtplus_gb300 import unbind as U
 
+    from hbtplus_gb300 import shard
+
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    batch, params = workload(args.nsub, rank, args.workload, args.open_angle, args.max_sample)
+    job, params = global_workload(args, ws)
+    job_sizes = np.diff(job["offsets"])
+    plan = shard.plan_shards(job_sizes, ws)
+    batch = shard.take(job, plan[rank])  # this rank's shard of the job
+    nsub_job = len(job_sizes)
     nsub = len(batch["offsets"]) - 1
     ntot = int(batch["offsets"][-1])
     prec = 1 if args.precision == "fp64" else 0
@@ -487,10 +615,14 @@ def main():
     def step():
         ub.unbind_batch_device(d_in, batch["offsets"], states, d_out)
 
-    # reference interactions/evaluations of this batch (identical walk): host call
-    _, _, host_res = ub.unbind_batch(batch)
-    interactions = sum(int(r["interactions"]) for r in host_res)
-    evaluations = sum(int(r["evaluations"]) for r in host_res)
+    # reference interactions/evaluations of the job (identical walk): a host call on
+    # this rank's shard, the shards' results gathered on rank 0 in job order
+    h_order, h_energy, host_res = ub.unbind_batch(batch)
+    tagged = [dict(r, _n=int(job_sizes[s])) for r, s in zip(host_res, plan[rank])]
+    gathered = shard.gather_results(plan, rank, ws, (h_order, h_energy, tagged))
+    job_res = gathered[2] if gathered is not None else []
+    interactions = sum(int(r["interactions"]) for r in job_res)
+    evaluations = sum(int(r["evaluations"]) for r in job_res)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -522,7 +654,7 @@ def main():
         total_ms = float(t.item())
         dist.barrier()
     ms_per_step = total_ms / args.steps
-    value = ws * nsub / (ms_per_step / 1e3)
+    value = nsub_job / (ms_per_step / 1e3)  # the whole job's subhaloes / the slowest rank
     clocks = clk.summary()
 
     # -- roofline of the dominant kernel launch: the first pass's energy walk ----
@@ -602,7 +734,7 @@ def main():
     h2d_ms, d2h_ms = copy_times(pin, d_in, [(out_order, d_out["order"]),
                                             (out_energy, d_out["energy"])],
                                 stream, args.steps)
-    e2e = {"value": ws * nsub / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+    e2e = {"value": nsub_job / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s,
            "h2d_ms": h2d_ms, "d2h_ms": d2h_ms,
            "copies_note": "h2d_ms / d2h_ms: the particle copies in and the order and energy "
@@ -611,7 +743,7 @@ def main():
 
     # -- plain form: one subhalo per call on the same GB300 ------------------------
     plain = None
-    if not args.no_plain and nsub > 1:
+    if not args.no_plain and nsub > 1 and ws == 1:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         order_np = np.empty(ntot, np.int64)
@@ -664,11 +796,11 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "scaling": args.scaling, "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded NFW/Jeans subhaloes, no public suite exists for this path)",
-        "config": config_of(args, batch),
-        "potentials_per_s": ws * evaluations / (ms_per_step / 1e3),
-        "interactions_per_s": ws * interactions / (ms_per_step / 1e3),
+        "config": config_of(args, job),
+        "potentials_per_s": evaluations / (ms_per_step / 1e3),
+        "interactions_per_s": interactions / (ms_per_step / 1e3),
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(st["kernel_launches"]),
         "clocks": clocks,
@@ -681,6 +813,12 @@ def main():
                               "passes": st["passes"] / args.steps,
                               "small_subhaloes": st["small_subhaloes"] / args.steps},
     }
+    line["config"]["parallelism"] = (f"{ws} rank(s), one GPU each: the job's {nsub_job} "
+                                     "subhaloes in LPT shards (hbtplus_gb300.shard), results "
+                                     "gathered on the host")
+    line["config"]["job_subhaloes"] = nsub_job
+    line["config"]["job_particles"] = int(job["offsets"][-1])
+    line["gathered_subhaloes"] = len(job_res)
     line["config"]["small_cutoff"] = small_cutoff
     line["config"]["small_blocks_per_sm"] = small_blocks
     if rank == 0:

@@ -33,6 +33,25 @@ def _states(ref_pos, ref_vel):
     return sts
 
 
+def bound_subset(batch: dict, order, results) -> dict:
+    """The bound particles of every subhalo of an unbound batch (most bound
+    first, as Unbind leaves Particles[0..Nbound)) with its final frame: the
+    fixed particle sets whose binding energy is differentiated.  ``order`` and
+    ``results`` are what Unbinder.unbind_batch returned for ``batch``."""
+    off = np.asarray(batch["offsets"], np.int64)
+    rows, counts = [], []
+    for s in range(len(off) - 1):
+        nb = int(results[s]["nbound"])
+        rows.append(int(off[s]) + np.asarray(order[int(off[s]):int(off[s]) + nb], np.int64))
+        counts.append(nb)
+    rows = np.concatenate(rows) if rows else np.zeros(0, np.int64)
+    out = {k: np.ascontiguousarray(np.asarray(batch[k])[rows]) for k in ("pos", "vel", "mass")}
+    out["offsets"] = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    out["ref_pos"] = np.array([r["ref_pos"] for r in results], np.float32).reshape(-1, 3)
+    out["ref_vel"] = np.array([r["ref_vel"] for r in results], np.float32).reshape(-1, 3)
+    return out
+
+
 def energy_gradient(ub: Unbinder, pos: torch.Tensor, vel: torch.Tensor, mass: torch.Tensor,
                     offsets, ref_pos, ref_vel, with_grad: bool = True):
     """E_tot per subhalo (float64, device) and, if asked, the gradients

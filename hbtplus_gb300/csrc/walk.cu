@@ -209,75 +209,97 @@ __global__ void __launch_bounds__(kWB) k_walk_fp64(Ctx c, int total)
 //   far  (r >= h): d(-m/r)/dx_t = -m dx / r^3,
 //   near (r < h):  d(m wp(u)/h)/dx_t = -m wp'(u) dx / (h^2 r),  u = r/h,
 // with wp' the derivative of the cubic-spline kernel; dx = x_node - x_target.
-__global__ void __launch_bounds__(kWB) k_grad_walk(Ctx c, int total)
+// The walk is walk_lean's (one target per lane, the same nodes in the same
+// order, the potential in the same compensated float sum); the gradient
+// terms go into float partial sums flushed into double every 16 steps, so a
+// target's results do not depend on the other targets of the call.  kGrad =
+// false computes only the energies (the forward pass of the autograd function).
+template <bool kSib, bool kGrad>
+__device__ __forceinline__ double walk_grad(const WNode *nodes, const Target &t,
+                                            const DevParams &P, double (&acc)[3])
+{
+  const float hf = (float)P.h, hinvf = (float)P.h_inv, h2f = hf * hf;
+  const double th2d = (double)P.theta2;
+  float hi = 0.f, comp = 0.f;  // Kahan sum of the potential
+  float ax = 0.f, ay = 0.f, az = 0.f;
+  acc[0] = acc[1] = acc[2] = 0.;
+  int iters = 0;
+  int cur = t.nxt;
+  const int end = t.end;
+  const int steps = kSib ? max(end - t.nxt, 0) : 0;
+  while (cur < end) {
+    float4 na;
+    int4 nm;
+    load_node(nodes, cur, na, nm);
+    const float dx = na.x - t.q[0], dy = na.y - t.q[1], dz = na.z - t.q[2];
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float lo = __int_as_float(nm.z);
+    const float up = kSib ? lo * kBandRatio : __int_as_float(nm.w);
+    bool open = r2 < lo;
+    if (r2 >= lo && r2 <= up)
+      open = exact_open(na, t.q[0], t.q[1], t.q[2], __int_as_float(nm.x & 0x7fffffff), th2d);
+    const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
+    const float mass = fabsf(na.w);  // cells carry their mass with the sign bit set
+    float contrib = -mass * rinv;
+    if (r2 < h2f) contrib = softened_fp32(mass, r2, rinv, hf, hinvf);
+    contrib = open ? 0.f : contrib;
+    const float y = __fsub_rn(contrib, comp);
+    const float sum = __fadd_rn(hi, y);
+    comp = __fsub_rn(__fsub_rn(sum, hi), y);
+    hi = sum;
+    if (kGrad && !open) {
+      float w;  // gradient weight: grad phi -= m * w * dx
+      if (r2 >= h2f) {
+        w = rinv * rinv * rinv;
+      } else {
+        const float u = r2 * rinv * hinvf;
+        const float iu = hf * rinv;  // 1/u
+        const float dwp = u < 0.5f
+                              ? u * (10.666666666667f + u * u * (32.0f * u - 38.4f))
+                              : -0.066666666667f * iu * iu +
+                                    u * (21.333333333333f +
+                                         u * (-48.0f + u * (38.4f - 10.666666666667f * u)));
+        w = r2 > 0.f ? hinvf * hinvf * dwp * rinv : 0.f;
+      }
+      const float mw = mass * w;
+      ax += mw * dx;
+      ay += mw * dy;
+      az += mw * dz;
+    }
+    iters++;
+    if (kGrad && (iters & 15) == 0) {
+      acc[0] += (double)ax;
+      acc[1] += (double)ay;
+      acc[2] += (double)az;
+      ax = ay = az = 0.f;
+    }
+    if (kSib) {
+      cur = open ? nm.w : nm.y;
+      if (iters >= steps || cur < t.nxt) break;  // malformed pointers: stop
+    } else {
+      cur = open ? cur + 1 : max(nm.y, cur + 1);
+    }
+  }
+  acc[0] += (double)ax;
+  acc[1] += (double)ay;
+  acc[2] += (double)az;
+  const double base = (double)__fdiv_rn(t.mself, P.eps);  // cancels the self term
+  return dadd(dadd(base, (double)hi), -(double)comp);
+}
+
+template <int kB, bool kSib, bool kGrad>
+__global__ void __launch_bounds__(kB) k_grad_walk(Ctx c, int total)
 {
   HBTU_KERNEL_PROLOGUE();
   const DevParams &P = c.P;
-  const unsigned full = 0xffffffffu;
   Target t;
-  load_target<true>(c, blockIdx.x * kWB + threadIdx.x, total, t);
-  double pot_d = (double)__fdiv_rn(t.mself, P.eps);
-  float pot_f = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
-  double axd = 0., ayd = 0., azd = 0.;
-  const float theta2 = P.theta2;
-  const float hf = (float)P.h, hinvf = (float)P.h_inv;
-  const double th2d = (double)P.theta2;
-  unsigned reduces = 0;
-  int cur = __reduce_min_sync(full, t.nxt);
-  while (cur != kDone) {
-    float4 na;
-    int2 nm;
-    load_node(c.nd, cur, na, nm);
-    if (t.nxt == cur) {
-      const float dx = na.x - t.q[0], dy = na.y - t.q[1], dz = na.z - t.q[2];
-      const float r2 = dx * dx + dy * dy + dz * dz;
-      if (opens(na, t.q, __int_as_float(nm.x & 0x7fffffff), r2, theta2, th2d)) {
-        t.nxt = cur + 1 < t.end ? cur + 1 : kDone;
-      } else {
-        const int sk = nm.y;
-        t.nxt = (unsigned)(sk - cur - 1) < (unsigned)(t.end - cur - 1) ? sk : kDone;
-        const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
-        const float r = r2 * rinv;
-        na.w = fabsf(na.w);  // cells carry their mass with the sign bit set
-        float w;  // gradient weight: accel += m * w * dx
-        if (r >= hf) {
-          pot_f -= na.w * rinv;
-          w = rinv * rinv * rinv;
-        } else {
-          const float u = r * hinvf;
-          float wp, dwp;
-          if (u < 0.5f) {
-            wp = -2.8f + u * u * (5.333333333333f + u * u * (6.4f * u - 9.6f));
-            dwp = u * (10.666666666667f + u * u * (32.0f * u - 38.4f));
-          } else {
-            wp = -3.2f + 0.066666666667f / u +
-                 u * u * (10.666666666667f + u * (-16.0f + u * (9.6f - 2.133333333333f * u)));
-            dwp = -0.066666666667f / (u * u) +
-                  u * (21.333333333333f + u * (-48.0f + u * (38.4f - 10.666666666667f * u)));
-          }
-          pot_f += na.w * hinvf * wp;
-          w = r2 > 0.f ? hinvf * hinvf * dwp * rinv : 0.f;
-        }
-        const float mw = na.w * w;
-        ax += mw * dx;
-        ay += mw * dy;
-        az += mw * dz;
-      }
-    }
-    cur = __reduce_min_sync(full, t.nxt);
-    if ((++reduces & 15u) == 0u) {
-      pot_d += (double)pot_f;
-      axd += (double)ax;
-      ayd += (double)ay;
-      azd += (double)az;
-      pot_f = ax = ay = az = 0.f;
-    }
-  }
+  load_target<true>(c, blockIdx.x * kB + threadIdx.x, total, t);
+  double acc[3];
+  const double pot_sum = walk_grad<kSib, kGrad>(kSib ? c.nd2 : c.nd, t, P, acc);
   if (!t.active) return;
   const SegState &sg = c.seg[t.s];
   const double ga = ddiv((double)P.G, (double)P.a);
-  const double pot = dmul(dadd(pot_d, (double)pot_f), ga);
-  const double gphi[3] = {-ga * (axd + ax), -ga * (ayd + ay), -ga * (azd + az)};
+  const double pot = dmul(pot_sum, ga);
   const float4 a = c.pm[t.pid], v = c.vel[t.pid];
   const float tp[3] = {a.x, a.y, a.z}, tv[3] = {v.x, v.y, v.z};
   float dv[3];
@@ -286,12 +308,25 @@ __global__ void __launch_bounds__(kWB) k_grad_walk(Ctx c, int total)
   const double k2 = (double)dv[0] * dv[0] + (double)dv[1] * dv[1] + (double)dv[2] * dv[2];
   const double ha = (double)P.Hz * (double)P.a;
   const int i = t.pid;  // no list permutation in this call: input position
-  if (c.grad_pos)
-    for (int j = 0; j < 3; j++) c.grad_pos[3 * i + j] = (float)(m * (ha * dv[j] + gphi[j]));
-  if (c.grad_vel)
-    for (int j = 0; j < 3; j++) c.grad_vel[3 * i + j] = (float)(m * dv[j]);
-  if (c.grad_mass) c.grad_mass[i] = (float)(0.5 * k2 + pot);
+  if (kGrad) {
+    if (c.grad_pos)
+      for (int j = 0; j < 3; j++) c.grad_pos[3 * i + j] = (float)(m * (ha * dv[j] - ga * acc[j]));
+    if (c.grad_vel)
+      for (int j = 0; j < 3; j++) c.grad_vel[3 * i + j] = (float)(m * dv[j]);
+    if (c.grad_mass) c.grad_mass[i] = (float)(0.5 * k2 + pot);
+  }
   c.e_part[i] = 0.5 * m * k2 + 0.5 * m * pot;
+}
+
+template <bool kSib, bool kGrad>
+void launch_grad(Ctx &c, int n)
+{
+  if (n >= 152 * 4 * 512)
+    launch_k(k_grad_walk<512, kSib, kGrad>, (n + 511) / 512, 512, 0, c.st, c, n);
+  else if (n >= 152 * 4 * 256)
+    launch_k(k_grad_walk<256, kSib, kGrad>, (n + 255) / 256, 256, 0, c.st, c, n);
+  else
+    launch_k(k_grad_walk<128, kSib, kGrad>, (n + 127) / 128, 128, 0, c.st, c, n);
 }
 
 }  // namespace
@@ -318,7 +353,16 @@ void launch_grad_walk(Ctx &c, const PassPlan &pl)
 {
   const int n = pl.ntgt_total;
   if (n <= 0) return;
-  launch_k(k_grad_walk, (n + kWB - 1) / kWB, kWB, 0, c.st, c, n);
+  const bool grad = c.grad_pos || c.grad_vel || c.grad_mass;
+  const bool sib = sibling_walk(c, pl);  // the tree build made the sibling-block records
+  if (sib && grad)
+    launch_grad<true, true>(c, n);
+  else if (sib)
+    launch_grad<true, false>(c, n);
+  else if (grad)
+    launch_grad<false, true>(c, n);
+  else
+    launch_grad<false, false>(c, n);
   HBTU_LAUNCHED();
 }
 

@@ -10,6 +10,8 @@ rank computes identically from the sizes alone.
     local = take(batch, plan[rank])                # this rank's sub-batch
     order, energy, results = unbinder.unbind_batch(local)
     merged = gather_results(plan, rank, world_size, (order, energy, results))
+
+or all of it in one call: unbind_sharded(unbinder, batch, rank, world_size).
 """
 from __future__ import annotations
 
@@ -87,3 +89,25 @@ def gather_results(plan, rank: int, world_size: int, local, group=None):
             pos += n
     return (np.concatenate(orders) if orders else np.zeros(0, np.int64),
             np.concatenate(energies) if energies else np.zeros(0, np.float32), results)
+
+
+def unbind_sharded(unbinder, batch: dict, rank: int, world_size: int, group=None):
+    """One batch unbound across world_size ranks: every rank plans the same
+    split, unbinds its own shard with ``unbinder.unbind_batch`` (one call on its
+    GPU, or any object with that method), and rank 0 gets the results of the
+    whole batch in batch order, as one unbind_batch call of the whole batch
+    would return them (None on the other ranks).  The only exchange is the
+    host-side gather of the results."""
+    sizes = np.diff(np.asarray(batch["offsets"], np.int64))
+    plan = plan_shards(sizes, world_size)
+    local = take(batch, plan[rank])
+    order, energy, results = unbinder.unbind_batch(local)
+    for k, s in enumerate(plan[rank]):
+        results[k] = dict(results[k], _n=int(sizes[s]))
+    out = gather_results(plan, rank, world_size, (order, energy, results), group=group)
+    if out is None:
+        return None
+    order, energy, results = out
+    for r in results:
+        r.pop("_n", None)
+    return order, energy, results

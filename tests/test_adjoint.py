@@ -11,7 +11,11 @@ Checks:
   * torch.autograd through BindingEnergy gives exactly the library's gradients;
   * one batched launch equals per-subhalo launches (to FP32 rounding);
   * the 1e6-particle subhalo: FP64 direct-sum gradients of 1000 random
-    particles, and momentum balance of sum m grad phi.
+    particles, and momentum balance of sum m grad phi;
+  * the bound sets of the 2000-subhalo batch after unbinding, differentiated
+    in one call: bit for bit the per-subhalo calls (each target's walk and
+    sums do not depend on the other subhaloes of a call), and within the
+    tree's error of FP64 direct-sum gradients on 1000 random particles.
 """
 import numpy as np
 import pytest
@@ -186,9 +190,8 @@ def test_autograd_and_batched_launch():
             a, z = int(off[s]), int(off[s + 1])
             Es, gp, gv, gm = energy_gradient(ub, pos[a:z], vel[a:z], mass[a:z], [0, z - a],
                                              b["ref_pos"][s:s + 1], b["ref_vel"][s:s + 1])
-            # FP32 partial sums are flushed on a warp-wide cadence, and the warps of a
-            # batch mix subhaloes: batched and single calls agree to FP32 rounding
-            assert abs(float(Es[0]) - float(E[s].detach())) <= 1e-6 * abs(float(Es[0]))
+            # each target's walk and sums are its own: batched and single calls agree
+            assert float(Es[0]) == float(E[s].detach())
             for got, ref in ((pos.grad[a:z], gp), (vel.grad[a:z], gv), (mass.grad[a:z], gm)):
                 ref = (ref * float(w[s])).cpu().numpy()
                 assert _rel(got.cpu().numpy(), ref) < 1e-5
@@ -225,3 +228,66 @@ def test_million_particle_subhalo_gradients():
     mg = gp.double() - mm[:, None] * HZ * (torch.tensor(sub["vel"], dtype=torch.float64,
                                                          device="cuda") - V + HZ * (x - X))
     assert float(mg.sum(0).norm()) <= 2e-3 * float(mg.norm(dim=1).sum())
+
+
+def test_batched_backward_of_the_2000_subhalo_batch():
+    """Config 3's batch form: the 2000-subhalo workload (867,289 particles)
+    unbound, then every subhalo's bound set differentiated in one call."""
+    import time
+
+    torch = pytest.importorskip("torch")
+    from hbtplus_gb300 import synthetic as S
+    from hbtplus_gb300.adjoint import bound_subset, energy_gradient
+    from hbtplus_gb300.unbind import Unbinder
+    batch = S.subhalo_batch(nsub=2000, seed=20261204)
+    p = S.default_params()
+    with Unbinder(p) as ub:
+        order, _, res = ub.unbind_batch(batch)
+        b = bound_subset(batch, order, res)
+        t = {k: torch.from_numpy(b[k]).cuda() for k in ("pos", "vel", "mass")}
+        E, gp, gv, gm = energy_gradient(ub, t["pos"], t["vel"], t["mass"], b["offsets"],
+                                        b["ref_pos"], b["ref_vel"])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            energy_gradient(ub, t["pos"], t["vel"], t["mass"], b["offsets"], b["ref_pos"],
+                            b["ref_vel"])
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / 3
+        print(f"batched backward: {len(b['mass'])} bound particles in 2000 subhaloes, "
+              f"{1e3 * dt:.2f} ms per call")
+        off = b["offsets"]
+        sizes = np.diff(off)
+        picks = list(np.argsort(sizes)[-5:]) + list(np.random.default_rng(8).choice(2000, 25))
+        for s in picks:
+            a, z = int(off[s]), int(off[s + 1])
+            if z - a == 0:
+                continue
+            Es, gps, gvs, gms = energy_gradient(ub, t["pos"][a:z], t["vel"][a:z], t["mass"][a:z],
+                                                [0, z - a], b["ref_pos"][s:s + 1],
+                                                b["ref_vel"][s:s + 1])
+            assert float(Es[0]) == float(E[s]), s
+            assert torch.equal(gps, gp[a:z]) and torch.equal(gvs, gv[a:z]), s
+            assert torch.equal(gms, gm[a:z]), s
+    # FP64 direct-sum gradients of 1000 random bound particles, each from its own
+    # subhalo's bound set (positions relative to the frame, periodic wrap)
+    rng = np.random.default_rng(9)
+    idx = np.sort(rng.choice(len(b["mass"]), 1000, replace=False))
+    sub_of = np.searchsorted(off, idx, side="right") - 1
+    got = gp[torch.as_tensor(idx, device="cuda")].double().cpu().numpy()
+    ref = np.empty_like(got)
+    for s in np.unique(sub_of):
+        a, z = int(off[s]), int(off[s + 1])
+        sel = idx[sub_of == s]
+        x = b["pos"][a:z].astype(np.float64) - b["ref_pos"][s].astype(np.float64)
+        x = np.where(x > 50.0, x - 100.0, np.where(x < -50.0, x + 100.0, x))
+        xt = torch.tensor(x, device="cuda")
+        m = torch.tensor(b["mass"][a:z], dtype=torch.float64, device="cuda")
+        v = torch.tensor(b["vel"][a:z], dtype=torch.float64, device="cuda")
+        V = torch.tensor(b["ref_vel"][s], dtype=torch.float64, device="cuda")
+        loc = torch.as_tensor(sel - a, device="cuda")
+        phi, gphi = direct(xt[loc], xt, m, 0.002, skip_self_index=loc)
+        dv = v[loc] - V + HZ * xt[loc]
+        ref[sub_of == s] = (m[loc][:, None] * (HZ * dv + gphi)).cpu().numpy()
+    print(f"batched backward vs FP64 direct sum on 1000 particles: rel L2 {_rel(got, ref):.2e}")
+    assert _rel(got, ref) < 2e-2

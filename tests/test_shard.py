@@ -80,6 +80,51 @@ def test_two_rank_gloo_shard_and_gather():
     assert imbalance < 1.05
 
 
+def _oracle_worker(rank, world, port, q):
+    """Each rank unbinds its shard with the C oracle (the stand-in for its
+    GPU); rank 0 compares the gathered batch with one oracle call on the whole
+    batch."""
+    import torch.distributed as dist
+    from helpers import OracleUnbinder
+    from oracle import Oracle
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    b = S.subhalo_batch(nsub=60, seed=12, nmax=3000)
+    p = S.default_params()
+    un = OracleUnbinder(Oracle(), p)
+    out = shard.unbind_sharded(un, b, rank, world)
+    if rank == 0:
+        order, energy, res = out
+        o1, e1, r1 = un.unbind_batch(b)
+        ok = np.array_equal(order, o1) and np.array_equal(energy, e1, equal_nan=True)
+        ok &= len(res) == len(r1)
+        for x, y in zip(res, r1):
+            for k in y:
+                ok &= np.array_equal(np.asarray(x[k]), np.asarray(y[k]), equal_nan=True)
+        q.put(bool(ok))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_sharded_unbinding_equals_one_rank():
+    """unbind_sharded over two gloo ranks gives, on rank 0, bit for bit the
+    results of unbinding the whole batch in one place."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_oracle_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    ok = q.get(timeout=300)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert ok
+
+
 def test_plan_is_a_partition_and_balanced():
     rng = np.random.Generator(np.random.PCG64(3))
     sizes = S.batch_sizes(rng, 2000)
