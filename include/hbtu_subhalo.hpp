@@ -11,6 +11,16 @@
 //   hbtu::DetectTrapsGPU(handle, subhaloes, snapshot, merged)
 //       replaces  FillHelpers + DetectTraps of SubhaloSnapshot_t::MergeSubhalos
 //                 (src/subhalo_merge.cpp:30-180, :193-199)
+//   hbtu::RecursiveUnbindGPU(handle, params, subhaloes, roots, snapshot)
+//       replaces  Subhalo_t::RecursiveUnbind from each root (src/subhalo_unbind.cpp:432-447),
+//                 one device call per nesting depth, deepest first
+//   hbtu::TruncateSource(subhalo, relax)
+//       replaces  Subhalo_t::TruncateSource (src/subhalo_unbind.cpp:449-458)
+//   hbtu::RefineParticlesGPU(handle, params, subhalo_snapshot, relax)
+//       replaces  SubhaloSnapshot_t::RefineParticles (src/subhalo_unbind.cpp:460-516)
+//   hbtu::MergeSubhalosGPU(handle, params, subhalo_snapshot, relax)
+//       replaces  SubhaloSnapshot_t::MergeSubhalos with MergeTrappedSubhalos on
+//                 (src/subhalo_merge.cpp:187-262)
 //
 // Templated on the caller's Subhalo_t / Snapshot_t, using the member names of
 // src/subhalo.h:24-146 and src/snapshot.h:51-111, so it compiles against the
@@ -26,6 +36,8 @@
 #include <algorithm>
 #include <cstdint>
 #include <type_traits>
+#include <unordered_set>
+#include <utility>
 #include <vector>
 
 #include "hbtu.h"
@@ -139,10 +151,15 @@ hbtu_status UnbindGPU(hbtu_handle *h, const hbtu_params &params, SubhaloT &sub,
 // The independent Unbind calls of one nesting level in one device call:
 // subhaloes[ids[k]] for every k (the field and new-born loops of
 // RefineParticles, src/subhalo_unbind.cpp:495-510).
+// `energies` (optional): Subhalo_t::Energies of each subhalo of the call, in
+// the order of `ids`.
 template <class SubhaloListT, class SnapshotT>
 hbtu_status UnbindBatchGPU(hbtu_handle *h, const hbtu_params &params, SubhaloListT &subhaloes,
-                           const std::vector<int64_t> &ids, const SnapshotT &epoch)
+                           const std::vector<int64_t> &ids, const SnapshotT &epoch,
+                           std::vector<std::vector<float>> *energies = nullptr)
 {
+  if (energies) energies->assign(ids.size(), std::vector<float>());
+  if (ids.empty()) return HBTU_OK;
   SubhaloArrays a;
   std::vector<int64_t> off(1, 0);
   std::vector<hbtu_state> st;
@@ -167,8 +184,118 @@ hbtu_status UnbindBatchGPU(hbtu_handle *h, const hbtu_params &params, SubhaloLis
   if (rc != HBTU_OK && rc != HBTU_ERR_NOT_CONVERGED) return rc;
   for (int64_t k = 0; k < nsub; k++)
     detail::apply(subhaloes[ids[k]], epoch, r[k], order.data() + off[k], energy.data() + off[k],
-                  (std::vector<float> *)nullptr);
+                  energies ? &(*energies)[k] : (std::vector<float> *)nullptr);
   return rc;
+}
+
+// Subhalo_t::TruncateSource (src/subhalo_unbind.cpp:449-458): Particles cut to
+// Nbound * SourceSubRelaxFactor (`relax`), the product formed in float and
+// truncated as the reference forms it (HBTInt times HBTReal).
+template <class SubhaloT>
+void TruncateSource(SubhaloT &s, float relax)
+{
+  int64_t n = (int64_t)s.Nbound;
+  if (n > 1) n = (int64_t)((float)s.Nbound * relax);
+  if (n > (int64_t)s.Particles.size()) n = (int64_t)s.Particles.size();
+  s.Particles.resize(n);
+}
+
+// Subhalo_t::RecursiveUnbind (src/subhalo_unbind.cpp:432-447) from each of
+// `roots`, for the whole forest below them: a nested subhalo is unbound before
+// its host, and its unbound tail (Particles[Nbound:]) is appended to the host's
+// list, in the order of NestedSubhalos, before the host is unbound; an orphan
+// (Nbound <= 1 on entry) is unbound on its own particles but keeps the
+// extended list to hand on.  The subhaloes of one nesting depth do not depend
+// on each other, so each depth is one hbtu_unbind_batch call, deepest first: a
+// forest costs one device call per level.  A subhalo listed in two nests is
+// unbound once, at its first appearance (depth-first order).
+template <class SubhaloListT, class SnapshotT>
+hbtu_status RecursiveUnbindGPU(hbtu_handle *h, const hbtu_params &params, SubhaloListT &subhaloes,
+                               const std::vector<int64_t> &roots, const SnapshotT &epoch)
+{
+  const int64_t nsub = (int64_t)subhaloes.size();
+  std::vector<int64_t> depth(nsub, -1);
+  int64_t maxd = -1;
+  std::vector<std::pair<int64_t, int64_t>> stack;
+  for (auto it = roots.rbegin(); it != roots.rend(); ++it) stack.emplace_back(*it, 0);
+  while (!stack.empty()) {  // depth-first preorder, first appearance wins
+    const auto top = stack.back();
+    stack.pop_back();
+    if (depth[top.first] >= 0) continue;
+    depth[top.first] = top.second;
+    maxd = std::max(maxd, top.second);
+    const auto &nest = subhaloes[top.first].NestedSubhalos;
+    for (auto it = nest.rbegin(); it != nest.rend(); ++it)
+      stack.emplace_back((int64_t)*it, top.second + 1);
+  }
+  hbtu_status worst = HBTU_OK;
+  for (int64_t d = maxd; d >= 0; d--) {
+    std::vector<int64_t> level;
+    for (int64_t s = 0; s < nsub; s++)
+      if (depth[s] == d) level.push_back(s);
+    std::vector<typename std::decay<decltype(subhaloes[0].Particles)>::type> extended;
+    std::vector<char> orphan(level.size());
+    for (size_t k = 0; k < level.size(); k++) {
+      auto &sub = subhaloes[level[k]];
+      orphan[k] = sub.Nbound <= 1;
+      auto ext = sub.Particles;
+      for (auto c : sub.NestedSubhalos) {
+        const auto &child = subhaloes[(int64_t)c];
+        if (depth[(int64_t)c] != d + 1) continue;  // unbound at another appearance
+        ext.insert(ext.end(), child.Particles.begin() + (int64_t)child.Nbound,
+                   child.Particles.end());
+      }
+      if (orphan[k]) {
+        extended.push_back(std::move(ext));  // its own particles are unbound
+      } else {
+        sub.Particles.swap(ext);
+        extended.emplace_back();
+      }
+    }
+    const hbtu_status rc = UnbindBatchGPU(h, params, subhaloes, level, epoch);
+    if (rc != HBTU_OK && rc != HBTU_ERR_NOT_CONVERGED) return rc;
+    if (rc != HBTU_OK) worst = rc;
+    for (size_t k = 0; k < level.size(); k++)
+      if (orphan[k]) subhaloes[level[k]].Particles.swap(extended[k]);  // :444-446
+  }
+  return worst;
+}
+
+// SubhaloSnapshot_t::RefineParticles (src/subhalo_unbind.cpp:460-516): each
+// halo's other top-level subhaloes join its central's nest, the forests of all
+// haloes go through RecursiveUnbindGPU together (one device call per depth),
+// the field and new-born subhaloes through one UnbindBatchGPU call, and every
+// list is cut by TruncateSource.  `relax` is SourceSubRelaxFactor.
+template <class SubhaloSnapshotT>
+hbtu_status RefineParticlesGPU(hbtu_handle *h, const hbtu_params &params, SubhaloSnapshotT &snap,
+                               float relax)
+{
+  auto &subs = snap.Subhalos;
+  auto &table = snap.MemberTable;
+  const int64_t nhalo = (int64_t)table.SubGroups.size();
+  std::vector<int64_t> roots, nest_size(nhalo, -1);
+  for (int64_t g = 0; g < nhalo; g++) {  // :481-494
+    const auto &group = table.SubGroups[g];
+    if (group.size() == 0) continue;
+    auto &nests = subs[(int64_t)group[0]].NestedSubhalos;
+    nest_size[g] = (int64_t)nests.size();
+    const auto &heads = table.SubGroupsOfHeads[g];
+    if (heads.size() > 1) nests.insert(nests.end(), heads.begin() + 1, heads.end());
+    roots.push_back((int64_t)group[0]);
+  }
+  const hbtu_status rc = RecursiveUnbindGPU(h, params, subs, roots, snap);
+  for (int64_t g = 0; g < nhalo; g++)  // restore the nests, also after an error
+    if (nest_size[g] >= 0) subs[(int64_t)table.SubGroups[g][0]].NestedSubhalos.resize(nest_size[g]);
+  if (rc != HBTU_OK && rc != HBTU_ERR_NOT_CONVERGED) return rc;
+  std::vector<int64_t> plain;  // field subhaloes, then new-born ones (:497-510)
+  const auto &field = table.SubGroups[-1];
+  for (int64_t i = 0; i < (int64_t)field.size(); i++) plain.push_back((int64_t)field[i]);
+  for (int64_t i = (int64_t)table.AllMembers.size(); i < (int64_t)subs.size(); i++)
+    plain.push_back(i);
+  const hbtu_status rc2 = UnbindBatchGPU(h, params, subs, plain, snap);
+  if (rc2 != HBTU_OK && rc2 != HBTU_ERR_NOT_CONVERGED) return rc2;
+  for (auto &s : subs) TruncateSource(s, relax);  // :511-512
+  return rc != HBTU_OK ? rc : rc2;
 }
 
 // Subhalo_t::CalculateProfileProperties and ::CalculateShape
@@ -288,6 +415,102 @@ hbtu_status DetectTrapsGPU(hbtu_handle *h, SubhaloListT &subhaloes, const Snapsh
     merged[i] = flag[i] != 0;
   }
   return HBTU_OK;
+}
+
+
+namespace detail {
+
+// Subhalo_t::MergeTo (src/subhalo_merge.cpp:244-262): the sink receives the
+// particles whose Ids it does not hold yet, in the subhalo's order, and the
+// subhalo's Nbound; the subhalo keeps its most-bound particle.
+template <class SubhaloT>
+void merge_to(SubhaloT &sat, SubhaloT &host)
+{
+  if (sat.Nbound <= 1) return;  // orphans and nulls
+  std::unordered_set<int64_t> ids(host.Particles.size() + sat.Particles.size());
+  for (const auto &p : host.Particles) ids.insert((int64_t)p.Id);
+  host.Particles.reserve(host.Particles.size() + sat.Particles.size());
+  for (const auto &p : sat.Particles)
+    if (ids.insert((int64_t)p.Id).second) host.Particles.push_back(p);
+  host.Nbound += sat.Nbound;
+  sat.Particles.resize(1);
+  sat.Nbound = 1;
+  sat.CountParticles();
+}
+
+// SubhaloSnapshot_t::MergeRecursive (:222-232): depth first, nested subhaloes
+// before their host; a trapped subhalo that is alive merges into its sink.
+template <class SubhaloListT>
+void merge_recursive(SubhaloListT &subs, int64_t root, int snapshot_index)
+{
+  std::vector<std::pair<int64_t, bool>> stack(1, std::make_pair(root, false));
+  while (!stack.empty()) {
+    const auto top = stack.back();
+    stack.pop_back();
+    auto &sat = subs[top.first];
+    if (!top.second) {
+      stack.emplace_back(top.first, true);
+      const auto &nest = sat.NestedSubhalos;
+      for (auto it = nest.rbegin(); it != nest.rend(); ++it)
+        stack.emplace_back((int64_t)*it, false);
+      continue;
+    }
+    if (sat.IsTrapped() && sat.IsAlive()) {
+      merge_to(sat, subs[(int64_t)sat.SinkTrackId]);
+      sat.SnapshotIndexOfDeath = snapshot_index;
+    }
+  }
+}
+
+}  // namespace detail
+
+// SubhaloSnapshot_t::MergeSubhalos with MergeTrappedSubhalos on
+// (src/subhalo_merge.cpp:187-220): the heads of each halo join its central's
+// nest (GlueHeadNests), DetectTrapsGPU finds the sinks on the device, trapped
+// subhaloes merge into their sinks depth first on the host, every subhalo that
+// swallowed one with Nbound > 1 is unbound again in one UnbindBatchGPU call and
+// cut by TruncateSource, and the nests are restored (UnglueHeadNests).
+// `energies` (optional): Subhalo_t::Energies of the re-unbound subhaloes
+// (empty for the others).
+template <class SubhaloSnapshotT>
+hbtu_status MergeSubhalosGPU(hbtu_handle *h, const hbtu_params &params, SubhaloSnapshotT &snap,
+                             float relax, std::vector<std::vector<float>> *energies = nullptr)
+{
+  auto &subs = snap.Subhalos;
+  auto &table = snap.MemberTable;
+  const int64_t nhalo = (int64_t)table.SubGroups.size();
+  std::vector<int64_t> nest_size(nhalo, -1);
+  for (int64_t g = 0; g < nhalo; g++) {  // GlueHeadNests (src/subhalo_tracking.cpp:843-862)
+    const auto &group = table.SubGroups[g];
+    if (group.size() == 0) continue;
+    auto &nests = subs[(int64_t)group[0]].NestedSubhalos;
+    nest_size[g] = (int64_t)nests.size();
+    const auto &heads = table.SubGroupsOfHeads[g];
+    if (heads.size() > 1) nests.insert(nests.end(), heads.begin() + 1, heads.end());
+  }
+  std::vector<char> merged;
+  hbtu_status rc = DetectTrapsGPU(h, subs, snap, merged);
+  std::vector<int64_t> again;
+  if (rc == HBTU_OK) {
+    const int isnap = (int)snap.GetSnapshotIndex();
+    for (int64_t g = 0; g < nhalo; g++)
+      if (table.SubGroups[g].size())
+        detail::merge_recursive(subs, (int64_t)table.SubGroups[g][0], isnap);
+    for (int64_t s = 0; s < (int64_t)subs.size(); s++)
+      if (merged[s]) again.push_back(s);
+  }
+  for (int64_t g = 0; g < nhalo; g++)  // UnglueHeadNests (:863-874)
+    if (nest_size[g] >= 0) subs[(int64_t)table.SubGroups[g][0]].NestedSubhalos.resize(nest_size[g]);
+  if (rc != HBTU_OK) return rc;
+  std::vector<std::vector<float>> en;
+  rc = UnbindBatchGPU(h, params, subs, again, snap, energies ? &en : nullptr);
+  if (rc != HBTU_OK && rc != HBTU_ERR_NOT_CONVERGED) return rc;
+  for (int64_t s : again) TruncateSource(subs[s], relax);
+  if (energies) {
+    energies->assign(subs.size(), std::vector<float>());
+    for (size_t k = 0; k < again.size(); k++) (*energies)[again[k]].swap(en[k]);
+  }
+  return rc;
 }
 
 }  // namespace hbtu

@@ -1,5 +1,11 @@
 """The C++ drop-in (include/hbtu_subhalo.hpp) used the way HBT+ would use it.
 
+Also, on the GPU: the nested caller (hbtu::RecursiveUnbindGPU + TruncateSource,
+and hbtu::RefineParticlesGPU with a member table) reproduces the reference's
+RecursiveUnbind forest (tests/golden/forest_10.npz), the merge caller
+(hbtu::MergeSubhalosGPU) the reference's MergeSubhalos (merge_10.npz), and a
+pass cap leaves a subhalo alike through UnbindGPU and UnbindBatchGPU.
+
 CPU: the shim compiles against stand-ins with the reference's member names
 (tests/shim/shim_lib.cpp) and, where the reference sources are present,
 against the reference's own headers.  GPU: the compiled harness unbinds golden
@@ -75,7 +81,8 @@ def test_shim_unbind_matches_reference(case):
                             *[C.c_void_p(arr[k].ctypes.data)
                               for k in ("id", "pos", "vel", "mass", "type")],
                             C.byref(st), C.c_void_p(out_id.ctypes.data),
-                            C.c_void_p(out_e.ctypes.data), C.byref(res), C.byref(death))
+                            C.c_void_p(out_e.ctypes.data), C.byref(res), C.byref(death),
+                            C.c_int32(0))
     assert rc == 0
     nb = int(ref["nbound"])
     assert res.nbound == nb and res.mbound == float(ref["mbound"])
@@ -161,3 +168,136 @@ def test_shim_detect_traps_match_reference():
     assert list(np.nonzero(snap == 7)[0]) == list(np.nonzero(newly)[0])
     want = {int(ref["sink"][s]) for s in np.nonzero(newly)[0] if st["nbound"][s] > 1}
     assert set(np.nonzero(merged)[0].tolist()) == want
+
+
+def _ptr(x):
+    return C.c_void_p(np.ascontiguousarray(x).ctypes.data)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [0, 1])
+def test_shim_forest_matches_reference(mode):
+    """forest_10 (two haloes with satellites three deep, an orphan with a
+    satellite, a satellite that disrupts, a field subhalo) through
+    hbtu::RecursiveUnbindGPU + TruncateSource (mode 0) and through
+    hbtu::RefineParticlesGPU with the haloes' member table (mode 1): the
+    reference's final lists and Nbound, FP64 mode, bit for bit."""
+    from hbtplus_gb300.unbind import Unbinder, params_from_dict
+    from test_refine import golden_forest
+    so = C.CDLL(build_shim())
+    forest, params, z = golden_forest()
+    nsub = len(forest["list_off"]) - 1
+    f = {k: np.ascontiguousarray(v) for k, v in forest.items()}
+    # the member table of mode 1: halo 0 is the tree of subhalo 0, halo 1 that of 7, and
+    # subhalo 9 (no nests, not an orphan) is a field subhalo
+    group_off = np.array([0, 7, 9], np.int64)
+    group_idx = np.array([0, 1, 2, 3, 4, 5, 6, 7, 8], np.int64)
+    heads_off = np.array([0, 1, 2], np.int64)
+    heads_idx = np.array([0, 7], np.int64)
+    field = np.array([9], np.int64)
+    cap = 4 * len(f["id"])
+    out_off = np.zeros(nsub + 1, np.int64)
+    out_row = np.zeros(cap, np.int64)
+    out_nb = np.zeros(nsub, np.int64)
+    cp = params_from_dict(params, precision=1)
+    keep = [out_off, out_row, out_nb, group_off, group_idx, heads_off, heads_idx, field]
+    with Unbinder(params, precision=1) as ub:
+        rc = so.shim_recursive_unbind(
+            ub.handle, C.byref(cp), C.c_int32(mode), C.c_int64(nsub), _ptr(f["list_off"]),
+            _ptr(f["id"]), _ptr(f["pos"]), _ptr(f["vel"]), _ptr(f["mass"]), _ptr(f["type"]),
+            _ptr(f["nbound_prev"]), _ptr(f["ref_pos"]), _ptr(f["ref_vel"]),
+            _ptr(f["mostbound_pos"]), _ptr(f["mostbound_vel"]), _ptr(f["nest_off"]),
+            _ptr(f["nest_idx"]), C.c_int64(len(f["roots"])), _ptr(f["roots"]),
+            C.c_int64(2), _ptr(group_off), _ptr(group_idx), _ptr(heads_off), _ptr(heads_idx),
+            C.c_int64(1), _ptr(field), C.c_float(float(z["relax"])), C.c_int64(cap),
+            _ptr(out_off), _ptr(out_row), _ptr(out_nb))
+    del keep
+    assert rc == 0, rc
+    assert list(out_nb) == list(z["ref_nbound"])
+    assert np.array_equal(out_off, z["ref_off"])
+    assert np.array_equal(out_row[:out_off[-1]], z["ref_pos_out"])
+
+
+@pytest.mark.gpu
+def test_shim_merge_matches_reference():
+    """merge_10 through hbtu::MergeSubhalosGPU (glued head nests, traps found
+    on the GPU, MergeTo depth first on the host, the merged hosts unbound again
+    in one batch and truncated), FP64 mode: the reference's lists, Nbound,
+    sinks and deaths."""
+    from hbtplus_gb300.unbind import Unbinder, params_from_dict
+    from helpers import tie_groups_equal
+    from test_merge import load
+    so = C.CDLL(build_shim())
+    par, st, ref, isnap, relax = load()
+    nsub = len(st["list_off"]) - 1
+    a = {k: np.ascontiguousarray(v) for k, v in st.items()}
+    a["sink"] = np.ascontiguousarray(a["sink"], np.int64)
+    a["death"] = np.ascontiguousarray(a["death"], np.int32)
+    cap = 4 * len(a["id"])
+    out_off = np.zeros(nsub + 1, np.int64)
+    out_id = np.zeros(cap, np.int64)
+    out_e = np.zeros(cap, np.float32)
+    nb = np.zeros(nsub, np.int64)
+    sink = np.zeros(nsub, np.int64)
+    sink_snap = np.zeros(nsub, np.int32)
+    death = np.zeros(nsub, np.int32)
+    cp = params_from_dict(par, precision=1)
+    nhalo = len(a["group_off"]) - 1
+    with Unbinder(par, precision=1) as ub:
+        rc = so.shim_merge_subhalos(
+            ub.handle, C.byref(cp), C.c_int64(nsub), _ptr(a["list_off"]), _ptr(a["id"]),
+            _ptr(a["pos"]), _ptr(a["vel"]), _ptr(a["mass"]), _ptr(a["type"]), _ptr(a["nbound"]),
+            _ptr(a["ref_pos"]), _ptr(a["ref_vel"]), _ptr(a["mostbound_pos"]),
+            _ptr(a["mostbound_vel"]), _ptr(a["nest_off"]), _ptr(a["nest_idx"]), C.c_int64(nhalo),
+            _ptr(a["group_off"]), _ptr(a["group_idx"]), _ptr(a["heads_off"]), _ptr(a["heads_idx"]),
+            _ptr(a["sink"]), _ptr(a["death"]), C.c_int32(isnap), C.c_float(relax),
+            C.c_int64(cap), _ptr(out_off), _ptr(out_id), _ptr(out_e), _ptr(nb), _ptr(sink),
+            _ptr(sink_snap), _ptr(death))
+    assert rc == 0, rc
+    assert list(nb) == list(ref["nbound"])
+    assert list(sink) == list(ref["sink"])
+    assert list(death) == list(ref["death"])
+    newly = ref["sink_snap"] >= 0
+    assert list(sink_snap[newly]) == list(ref["sink_snap"][newly])
+    for s in range(nsub):
+        got = out_id[out_off[s]:out_off[s + 1]]
+        want = ref["id"][ref["off"][s]:ref["off"][s + 1]]
+        e = out_e[out_off[s]:out_off[s + 1]]
+        if np.isnan(e).all():
+            assert np.array_equal(got, want), s
+        else:  # unbound again: bound part up to runs of equal energy, tail exact
+            k = int(np.sum(~np.isnan(e)))
+            assert tie_groups_equal(got[:k], want[:k], e[:k]), s
+            assert np.array_equal(got[k:], want[k:]), s
+
+
+@pytest.mark.gpu
+def test_shim_pass_cap_leaves_single_and_batch_forms_alike():
+    """With max_passes reached, hbtu::UnbindGPU and hbtu::UnbindBatchGPU both
+    return HBTU_ERR_NOT_CONVERGED and leave the subhalo in the same state (the
+    last pass's order, Nbound and frame)."""
+    from hbtplus_gb300 import _lib
+    from hbtplus_gb300.unbind import Unbinder, _state, params_from_dict
+    so = C.CDLL(build_shim())
+    par, inp, _ = load_case("nfw_1100")
+    n = len(inp["mass"])
+    cp = params_from_dict(par, precision=1, max_passes=1)
+    st = _state(inp["ref_pos"], inp["ref_vel"], inp["mostbound_pos"], inp["mostbound_vel"],
+                inp["id"][0])
+    arr = {k: np.ascontiguousarray(inp[k]) for k in ("id", "pos", "vel", "mass", "type")}
+    outs = []
+    with Unbinder(par, precision=1, max_passes=1) as ub:
+        for via_batch in (0, 1):
+            out_id = np.zeros(n, np.int64)
+            out_e = np.zeros(n, np.float32)
+            res = _lib.hbtu_result()
+            death = C.c_int32(0)
+            rc = so.shim_unbind(ub.handle, C.byref(cp), C.c_int64(n),
+                                *[_ptr(arr[k]) for k in ("id", "pos", "vel", "mass", "type")],
+                                C.byref(st), _ptr(out_id), _ptr(out_e), C.byref(res),
+                                C.byref(death), C.c_int32(via_batch))
+            assert rc == _lib.HBTU_ERR_NOT_CONVERGED
+            outs.append((out_id.copy(), res.nbound, res.mbound, list(res.ref_pos)))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert outs[0][1:] == outs[1][1:]
+    assert not np.array_equal(outs[0][0], arr["id"])  # the last pass's order was applied
