@@ -471,11 +471,34 @@ def run_adjoint(args, ws, rank, local):
     npart = int(b["offsets"][-1])
     T = {k: torch.from_numpy(b[k]).to(dev) for k in ("pos", "vel", "mass")}
     stream = torch.cuda.current_stream(dev)
+    ub.set_stream(stream.cuda_stream)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    off = np.ascontiguousarray(b["offsets"], np.int64)
+    sts = (_lib.hbtu_state * nsub)()
+    for s in range(nsub):
+        sts[s] = _state(b["ref_pos"][s], b["ref_vel"][s], b["ref_pos"][s], b["ref_vel"][s], -1)
+    # the timed call: device-resident inputs and outputs through the C ABI
+    d_ids = torch.arange(npart, dtype=torch.int64, device=dev)
+    d_E = torch.empty(nsub, dtype=torch.float64, device=dev)
+    d_g = [torch.empty((npart, 3), dtype=torch.float32, device=dev),
+           torch.empty((npart, 3), dtype=torch.float32, device=dev),
+           torch.empty(npart, dtype=torch.float32, device=dev)]
+    p_dev = _lib.hbtu_particles(id=d_ids.data_ptr(), pos=T["pos"].data_ptr(),
+                                vel=T["vel"].data_ptr(), mass=T["mass"].data_ptr(), type=0,
+                                location=_lib.HBTU_DEVICE, reserved=0)
 
     def step():
-        return energy_gradient(ub, T["pos"], T["vel"], T["mass"], b["offsets"], b["ref_pos"],
-                               b["ref_vel"])
+        rc = ub.lib.hbtu_energy_gradient(ub.handle, C.byref(p_dev), nsub, off.ctypes.data,
+                                         C.addressof(sts), d_E.data_ptr(), d_g[0].data_ptr(),
+                                         d_g[1].data_ptr(), d_g[2].data_ptr())
+        _lib.check(rc, ub.handle)
+
+    # the same gradient as the autograd path's (hbtplus_gb300.adjoint)
+    _, gp_ref, _, _ = energy_gradient(ub, T["pos"], T["vel"], T["mass"], b["offsets"],
+                                      b["ref_pos"], b["ref_vel"])
+    step()
+    torch.cuda.synchronize()
+    assert torch.equal(gp_ref, d_g[0])
 
     for _ in range(args.warmup):
         step()
@@ -501,10 +524,6 @@ def run_adjoint(args, ws, rank, local):
     gv = torch.empty((npart, 3), dtype=torch.float32).pin_memory()
     gm = torch.empty(npart, dtype=torch.float32).pin_memory()
     E = np.zeros(nsub, np.float64)
-    off = np.ascontiguousarray(b["offsets"], np.int64)
-    sts = (_lib.hbtu_state * nsub)()
-    for s in range(nsub):
-        sts[s] = _state(b["ref_pos"][s], b["ref_vel"][s], b["ref_pos"][s], b["ref_vel"][s], -1)
     p_host = _lib.hbtu_particles(id=ids.data_ptr(), pos=pin["pos"].data_ptr(),
                                  vel=pin["vel"].data_ptr(), mass=pin["mass"].data_ptr(), type=0,
                                  location=_lib.HBTU_HOST, reserved=0)

@@ -716,6 +716,7 @@ hbtu_status hbtu_energy_gradient(hbtu_handle *h, const hbtu_particles *p, int64_
     Ctx c;
     Staging sg;
     bool host = true;
+    const long long launches0 = g_launches;
     // a single full pass over every particle: no sampling
     const int64_t saved = h->params.max_sample_size;
     h->params.max_sample_size = 0;
@@ -759,6 +760,7 @@ hbtu_status hbtu_energy_gradient(hbtu_handle *h, const hbtu_particles *p, int64_
                                   cudaMemcpyDeviceToHost, c.st));
     }
     HBTU_CUDA(cudaStreamSynchronize(c.st));
+    h->stats.kernel_launches += g_launches - launches0;
     return HBTU_OK;
   } catch (const CudaError &e) {
     return fail(h, HBTU_ERR_CUDA, e.what);
