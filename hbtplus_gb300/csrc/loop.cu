@@ -458,27 +458,11 @@ __global__ void __launch_bounds__(kLB) k_avg_chunks(Ctx c)
   const int ci = b - c.bchunk_base[s];
   const int lo = ci * kChunk, hi = min(lo + kChunk, nb);
   const float4 o = c.pm[c.epid[sg.off]];
-  const double ox = f2d(o.x), oy = f2d(o.y), oz = f2d(o.z);
+  const double od[3] = {f2d(o.x), f2d(o.y), f2d(o.z)};
   double v[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int p = lo + threadIdx.x; p < hi; p += kLB) {
     const int pid = c.epid[sg.off + p];
-    const float4 a = c.pm[pid];
-    const float4 u = c.vel[pid];
-    const float m = a.w;
-    const double md = f2d(m);
-    v[0] += md;
-    v[1] += f2d(fmul(u.x, m));
-    v[2] += f2d(fmul(u.y, m));
-    v[3] += f2d(fmul(u.z, m));
-    if (c.P.periodic) {
-      v[4] += dmul(nearest_d(dsub(f2d(a.x), ox), c.P), md);
-      v[5] += dmul(nearest_d(dsub(f2d(a.y), oy), c.P), md);
-      v[6] += dmul(nearest_d(dsub(f2d(a.z), oz), c.P), md);
-    } else {
-      v[4] += f2d(fmul(a.x, m));
-      v[5] += f2d(fmul(a.y, m));
-      v[6] += f2d(fmul(a.z, m));
-    }
+    frame_terms(c.pm[pid], c.vel[pid], o, od, c.P, v);
   }
   block_sum<7>(v, c.chunk_sums + (size_t)b * kSums, hi - lo);
 }

@@ -82,6 +82,52 @@ __device__ void block_sum(double (&v)[K], double *out, int nvalid)
   }
 }
 
+// NEAREST(x - o) * m in double (AveragePosition's term, src/subhalo_unbind.cpp:
+// 139-188), bit for bit, mostly without double arithmetic.  When the float
+// difference s = x - o is exact (a float TwoSum with a zero error term) and
+// |s| < box, the wrap s -+ box is exact in float too (Sterbenz: box/2 < |s| <
+// 2 box), and the product of the two floats is exact as a float product plus
+// its fma remainder, added exactly in double: one FP64 add instead of the
+// double subtract, wrap and multiply (FP64 runs at 1/64 of the FP32 rate on
+// this GPU).  Otherwise the double path.
+__device__ __forceinline__ double rel_times_mass(float x, float o, double od, float m, double md,
+                                                 const DevParams &P)
+{
+  const float s = __fsub_rn(x, o);
+  const float bb = __fsub_rn(s, x);
+  const float err = __fadd_rn(__fsub_rn(x, __fsub_rn(s, bb)), __fsub_rn(-o, bb));
+  if (err == 0.f && fabsf(s) < P.box) {
+    const float q = s > P.boxhalf ? __fsub_rn(s, P.box) : (s < -P.boxhalf ? __fadd_rn(s, P.box) : s);
+    const float p = __fmul_rn(q, m);
+    const float r = __fmaf_rn(q, m, -p);  // q*m - p, exact
+    return dadd(f2d(p), f2d(r));
+  }
+  return dmul(nearest_d(dsub(f2d(x), od), P), md);
+}
+
+// One bound particle's terms of the frame sums: w[0] += m, w[1..3] += v*m
+// (float products), w[4..6] += NEAREST(x - o)*m about the origin o (periodic)
+// or x*m (float products).
+__device__ __forceinline__ void frame_terms(float4 a, float4 u, float4 o, const double (&od)[3],
+                                            const DevParams &P, double (&w)[7])
+{
+  const float m = a.w;
+  const double md = f2d(m);
+  w[0] += md;
+  w[1] += f2d(fmul(u.x, m));
+  w[2] += f2d(fmul(u.y, m));
+  w[3] += f2d(fmul(u.z, m));
+  if (P.periodic) {
+    w[4] += rel_times_mass(a.x, o.x, od[0], m, md, P);
+    w[5] += rel_times_mass(a.y, o.y, od[1], m, md, P);
+    w[6] += rel_times_mass(a.z, o.z, od[2], m, md, P);
+  } else {
+    w[4] += f2d(fmul(a.x, m));
+    w[5] += f2d(fmul(a.y, m));
+    w[6] += f2d(fmul(a.z, m));
+  }
+}
+
 // The decisions of subhalo s after a pass whose partition kept nb particles
 // bound; v[0..6] are the bound block's sums (mass, mass-weighted velocity,
 // mass-weighted position about Elist[0]) when nb > 1.

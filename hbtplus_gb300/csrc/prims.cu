@@ -103,6 +103,68 @@ __device__ __forceinline__ unsigned rs_digit(unsigned hi, unsigned long long lo,
   return word ? (hi >> shift) & 255u : (unsigned)(lo >> shift) & 255u;
 }
 
+// Stable ranking of a block's records by digit, each warp owning a run of
+// consecutive records (round r of warp w holds its records r*32 .. r*32+31):
+// within a round __match_any_sync groups the lanes of one digit, and a
+// per-warp count per digit carries the rank across rounds, so the records of
+// a warp are ranked without block barriers.  rk[r] is the record's rank among
+// the warp's records of its digit; wcnt[w][d] ends as the warp's count of d.
+// Lanes without a record pass a unique sentinel digit (256 + lane).
+template <int kRounds>
+__device__ __forceinline__ void warp_rank(const unsigned (&dg)[kRounds], unsigned (&rk)[kRounds],
+                                          unsigned (*wcnt)[256])
+{
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int r = 0; r < kRounds; r++) {
+    const unsigned d = dg[r];
+    const unsigned mask = __match_any_sync(0xffffffffu, d);
+    const unsigned before = __popc(mask & lt);
+    const bool real = d < 256u;
+    const unsigned base = real ? wcnt[warp][d] : 0u;
+    __syncwarp();
+    if (real && before == 0) wcnt[warp][d] = base + __popc(mask);
+    __syncwarp();
+    rk[r] = base + before;
+  }
+}
+
+// After warp_rank: the warps' counts become the warps' offsets within each
+// digit (wcnt[w][d] = records of digit d in warps before w), and the return
+// value is the block's count of digit threadIdx.x (kBlock == 256 threads,
+// one digit each).
+__device__ __forceinline__ unsigned warp_offsets(unsigned (*wcnt)[256])
+{
+  const int t = threadIdx.x;
+  unsigned run = 0;
+#pragma unroll
+  for (int w = 0; w < kBlock / 32; w++) {
+    const unsigned c = wcnt[w][t];
+    wcnt[w][t] = run;
+    run += c;
+  }
+  return run;
+}
+
+// Exclusive scan over the block of one value per thread (kBlock threads).
+__device__ __forceinline__ unsigned block_excl_scan_u32(unsigned v, unsigned *wsum)
+{
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  unsigned before = 0;
+  for (int w = 0; w < warp; w++) before += wsum[w];
+  __syncthreads();
+  return before + x - v;
+}
+
 // Every pass of a sort of at most kSmallN records in one block, the records
 // held in shared memory between passes: the same stable histogram /
 // scan / ranked-scatter steps as the multi-block passes, without a launch
@@ -122,82 +184,45 @@ __global__ void __launch_bounds__(kBlock) k_rs_small(unsigned *hi_g, unsigned lo
   unsigned long long *const lo0 = (unsigned long long *)smem;
   unsigned *const hi0 = (unsigned *)(lo0 + 2 * kSmallN);
   int *const val0 = (int *)(hi0 + 2 * kSmallN);
-  __shared__ unsigned hist[256];
   __shared__ unsigned wcnt[kBlock / 32][256];
-  __shared__ unsigned run_base[256];
+  __shared__ unsigned toff[256];
+  __shared__ unsigned wsum[kBlock / 32];
+  constexpr int kRounds = kSmallN / kBlock;  // records per lane: warp w owns [w*32*kRounds, ..)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int e = tid; e < n; e += kBlock) {
     lo0[e] = lo_g[e];
     hi0[e] = hi_g[e];
     val0[e] = val_g[e];
   }
-  const unsigned lt = (1u << lane) - 1u;
   int cur = 0;
   for (int p = 0; p < ps.n; p++) {
     const int word = ps.words[p], shift = ps.shifts[p];
-    hist[tid] = 0;
-    run_base[tid] = 0;
 #pragma unroll
     for (int w = 0; w < kBlock / 32; w++) wcnt[w][tid] = 0;
     __syncthreads();
-    for (int e = tid; e < n; e += kBlock)
-      atomicAdd(&hist[rs_digit(word ? hi0[cur * kSmallN + e] : 0u, word ? 0ull : lo0[cur * kSmallN + e], word, shift)], 1u);
-    __syncthreads();
-    {  // exclusive scan of the 256 digit counts (thread tid owns digit tid)
-      const unsigned v = hist[tid];
-      unsigned x = v;
+    unsigned dg[kRounds], rk[kRounds];
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-      }
-      __shared__ unsigned wsum[kBlock / 32];
-      if (lane == 31) wsum[warp] = x;
-      __syncthreads();
-      unsigned before = 0;
-      for (int w = 0; w < warp; w++) before += wsum[w];
-      __syncthreads();
-      hist[tid] = before + x - v;  // start of digit tid
+    for (int r = 0; r < kRounds; r++) {
+      const int e = warp * 32 * kRounds + r * 32 + lane;
+      dg[r] = e < n ? rs_digit(hi0[cur * kSmallN + e], lo0[cur * kSmallN + e], word, shift)
+                    : 256u + lane;
+    }
+    warp_rank<kRounds>(dg, rk, wcnt);
+    __syncthreads();
+    const unsigned cnt = warp_offsets(wcnt);
+    toff[tid] = block_excl_scan_u32(cnt, wsum);  // start of digit tid
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kRounds; r++) {
+      const int e = warp * 32 * kRounds + r * 32 + lane;
+      if (e >= n) continue;
+      const unsigned d = dg[r];
+      const unsigned dst = toff[d] + wcnt[warp][d] + rk[r];
+      hi0[(cur ^ 1) * kSmallN + dst] = hi0[cur * kSmallN + e];
+      lo0[(cur ^ 1) * kSmallN + dst] = lo0[cur * kSmallN + e];
+      val0[(cur ^ 1) * kSmallN + dst] = val0[cur * kSmallN + e];
     }
     __syncthreads();
-    for (int r = 0; r * kBlock < n; r++) {
-      const int e = r * kBlock + tid;
-      const bool valid = e < n;
-      unsigned h = 0, d = 256u + lane;  // unique sentinel for invalid lanes
-      unsigned long long l = 0;
-      int v = 0;
-      if (valid) {
-        h = hi0[cur * kSmallN + e];
-        l = lo0[cur * kSmallN + e];
-        v = val0[cur * kSmallN + e];
-        d = rs_digit(h, l, word, shift);
-      }
-      const unsigned mask = __match_any_sync(0xffffffffu, d);
-      const unsigned rank = __popc(mask & lt);
-      if (valid && rank == 0) wcnt[warp][d] = __popc(mask);
-      __syncthreads();
-      {
-        unsigned run = run_base[tid];
-#pragma unroll
-        for (int w = 0; w < kBlock / 32; w++) {
-          const unsigned t = wcnt[w][tid];
-          wcnt[w][tid] = run;
-          run += t;
-        }
-        run_base[tid] = run;
-      }
-      __syncthreads();
-      if (valid) {
-        const unsigned dst = hist[d] + wcnt[warp][d] + rank;
-        hi0[(cur ^ 1) * kSmallN + dst] = h;
-        lo0[(cur ^ 1) * kSmallN + dst] = l;
-        val0[(cur ^ 1) * kSmallN + dst] = v;
-      }
-      __syncthreads();
-#pragma unroll
-      for (int w = 0; w < kBlock / 32; w++) wcnt[w][tid] = 0;
-      __syncthreads();
-    }
     cur ^= 1;
   }
   for (int e = tid; e < n; e += kBlock) {
@@ -280,8 +305,6 @@ __global__ void __launch_bounds__(kBlock) k_os_pass(
 {
   HBTU_KERNEL_PROLOGUE();
   __shared__ unsigned wcnt[kBlock / 32][256];
-  __shared__ unsigned run_base[256];
-  __shared__ unsigned hist[256];
   __shared__ unsigned toff[256];  // first slot of each digit in the tile's sorted order
   __shared__ unsigned base[256];
   __shared__ unsigned wsum[kBlock / 32];
@@ -291,82 +314,47 @@ __global__ void __launch_bounds__(kBlock) k_os_pass(
   __shared__ int tile_s;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) tile_s = atomicAdd(tile_counter, 1);
-  hist[tid] = 0;
-  run_base[tid] = 0;
 #pragma unroll
   for (int w = 0; w < kBlock / 32; w++) wcnt[w][tid] = 0;
   __syncthreads();
   const int tile = tile_s;
   const long long t0 = (long long)tile * kTile;
-  // this tile's digits
-  unsigned dg[kItems];
+  // this tile's records: warp w holds tile positions w*256 .. w*256+255, lane-contiguous
+  unsigned dg[kItems], rk[kItems], hv[kItems];
+  unsigned long long lv[kItems];
+  int vv[kItems];
 #pragma unroll
   for (int r = 0; r < kItems; r++) {
-    const long long e = t0 + r * kBlock + tid;
-    dg[r] = 256u;
+    const long long e = t0 + warp * 32 * kItems + r * 32 + lane;
+    dg[r] = 256u + lane;  // unique sentinel for lanes past the end
+    hv[r] = 0;
+    lv[r] = 0;
+    vv[r] = 0;
     if (e < n) {
-      dg[r] = rs_digit(hi_in[e], lo_in[e], word, shift);
-      atomicAdd(&hist[dg[r]], 1u);
+      hv[r] = hi_in[e];
+      lv[r] = lo_in[e];
+      vv[r] = val_in[e];
+      dg[r] = rs_digit(hv[r], lv[r], word, shift);
     }
   }
+  warp_rank<kItems>(dg, rk, wcnt);
   __syncthreads();
+  const unsigned cnt = warp_offsets(wcnt);
   // publish this tile's counts at once, so later tiles can look back past it
   volatile unsigned *st = status;
-  const unsigned cnt = hist[tid];
   st[(long long)tile * 256 + tid] = (tile == 0 ? kFlagPre : kFlagAgg) | cnt;
-  {  // tile-local exclusive offsets of the digits
-    unsigned x = cnt;
+  toff[tid] = block_excl_scan_u32(cnt, wsum);  // tile-local start of each digit
+  __syncthreads();
+  // stable local sort of the tile into shared memory
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) wsum[warp] = x;
-    __syncthreads();
-    unsigned before = 0;
-    for (int w = 0; w < warp; w++) before += wsum[w];
-    toff[tid] = before + x - cnt;
-  }
-  // stable local sort of the tile into shared memory (ranks in element order)
-  const unsigned lt = (1u << lane) - 1u;
   for (int r = 0; r < kItems; r++) {
-    const long long e = t0 + r * kBlock + tid;
-    const bool valid = e < n;
-    unsigned h = 0;
-    unsigned long long l = 0;
-    int v = 0;
-    const unsigned d = valid ? dg[r] : 256u + lane;  // unique sentinel for invalid lanes
-    if (valid) {
-      h = hi_in[e];
-      l = lo_in[e];
-      v = val_in[e];
-    }
-    const unsigned mask = __match_any_sync(0xffffffffu, d);
-    const unsigned rank = __popc(mask & lt);
-    if (valid && rank == 0) wcnt[warp][d] = __popc(mask);
-    __syncthreads();
-    {
-      unsigned run = run_base[tid];
-#pragma unroll
-      for (int w = 0; w < kBlock / 32; w++) {
-        const unsigned t = wcnt[w][tid];
-        wcnt[w][tid] = run;
-        run += t;
-      }
-      run_base[tid] = run;
-    }
-    __syncthreads();
-    if (valid) {
-      const unsigned slot = toff[d] + wcnt[warp][d] + rank;
-      s_hi[slot] = h;
-      s_lo[slot] = l;
-      s_val[slot] = v;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int w = 0; w < kBlock / 32; w++) wcnt[w][tid] = 0;
-    __syncthreads();
+    if (dg[r] >= 256u) continue;
+    const unsigned slot = toff[dg[r]] + wcnt[warp][dg[r]] + rk[r];
+    s_hi[slot] = hv[r];
+    s_lo[slot] = lv[r];
+    s_val[slot] = vv[r];
   }
+  __syncthreads();
   // look back for the earlier tiles' total of each digit
   unsigned prefix = 0;
   for (int k = tile - 1; k >= 0;) {

@@ -405,30 +405,14 @@ __device__ void frame_sums(const Ctx &c, const SegState &sg, int nb, double *chu
   for (int k = 0; k < 7; k++) v[k] = 0.;
   if (nb <= 1) return;
   const float4 o = c.pm[c.epid[sg.off]];
-  const double ox = f2d(o.x), oy = f2d(o.y), oz = f2d(o.z);
+  const double od[3] = {f2d(o.x), f2d(o.y), f2d(o.z)};
   const int nch = (nb + kChunk - 1) / kChunk;
   for (int ci = 0; ci < nch; ci++) {
     const int lo = ci * kChunk, hi = min(lo + kChunk, nb);
     double w[7] = {0, 0, 0, 0, 0, 0, 0};
     for (int p = lo + threadIdx.x; p < hi; p += kLB) {
       const int pid = c.epid[sg.off + p];
-      const float4 a = c.pm[pid];
-      const float4 u = c.vel[pid];
-      const float m = a.w;
-      const double md = f2d(m);
-      w[0] += md;
-      w[1] += f2d(fmul(u.x, m));
-      w[2] += f2d(fmul(u.y, m));
-      w[3] += f2d(fmul(u.z, m));
-      if (c.P.periodic) {
-        w[4] += dmul(nearest_d(dsub(f2d(a.x), ox), c.P), md);
-        w[5] += dmul(nearest_d(dsub(f2d(a.y), oy), c.P), md);
-        w[6] += dmul(nearest_d(dsub(f2d(a.z), oz), c.P), md);
-      } else {
-        w[4] += f2d(fmul(a.x, m));
-        w[5] += f2d(fmul(a.y, m));
-        w[6] += f2d(fmul(a.z, m));
-      }
+      frame_terms(c.pm[pid], c.vel[pid], o, od, c.P, w);
     }
     block_sum<7>(w, chunk + (size_t)ci * kSums, hi - lo);
     __syncthreads();
