@@ -79,9 +79,6 @@ def parse():
                          "1000 the reference's production default")
     ap.add_argument("--walk-layout", type=int, default=-1,
                     help="walk_layout option of the FP32 walk (-1: library default)")
-    ap.add_argument("--walk-stage", type=int, default=-1,
-                    help="walk_stage_depth option: nodes down to this depth read from "
-                         "shared memory (-1: library default, 0: off)")
     ap.add_argument("--walk-schedule", type=int, default=-1,
                     help="walk_schedule option of the FP32 walk (-1: library default)")
     ap.add_argument("--small-cutoff", type=int, default=-1,
@@ -614,15 +611,12 @@ def main():
         ub.set_option("walk_schedule", args.walk_schedule)
     if args.walk_layout >= 0:
         ub.set_option("walk_layout", args.walk_layout)
-    if args.walk_stage >= 0:
-        ub.set_option("walk_stage_depth", args.walk_stage)
     if args.small_cutoff >= 0:
         ub.set_option("small_cutoff", args.small_cutoff)
     if args.small_blocks >= 0:
         ub.set_option("small_blocks_per_sm", args.small_blocks)
     small_cutoff = ub.get_option("small_cutoff")
     small_blocks = ub.get_option("small_blocks_per_sm")
-    walk_stage = ub.get_option("walk_stage_depth")
 
     stream = torch.cuda.current_stream(dev)
     ub.set_stream(stream.cuda_stream)
@@ -846,7 +840,6 @@ def main():
     line["gathered_subhaloes"] = len(job_res)
     line["config"]["small_cutoff"] = small_cutoff
     line["config"]["small_blocks_per_sm"] = small_blocks
-    line["config"]["walk_stage_depth"] = walk_stage
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -254,7 +254,6 @@ hbtu_status setup_call(hbtu_handle *h, const hbtu_particles *p, long long S, con
   c.opt_leaf_runs = (int)h->opt_leaf_runs;
   c.opt_schedule = (int)h->opt_schedule;
   c.opt_layout = (int)h->opt_layout;
-  c.stage_depth = (int)h->opt_stage;
   std::vector<SegState> segs;
   std::vector<int> segoff, order(S);
   init_states(h, S, offsets, st, segs, segoff);
@@ -568,13 +567,6 @@ hbtu_status hbtu_set_option(hbtu_handle *h, const char *name, int64_t value)
     h->opt_layout = value;
     return HBTU_OK;
   }
-  if (n == "walk_stage_depth") {
-    if (value < 0 || value > kStageMaxDepth)
-      return fail(h, HBTU_ERR_INVALID_ARGUMENT,
-                  "walk_stage_depth: 0 (off) to " + std::to_string(kStageMaxDepth));
-    h->opt_stage = value;
-    return HBTU_OK;
-  }
   if (n == "small_cutoff") {
     if (value < 0 || value > kSmallCap)
       return fail(h, HBTU_ERR_INVALID_ARGUMENT,
@@ -605,10 +597,6 @@ hbtu_status hbtu_get_option(const hbtu_handle *h, const char *name, int64_t *val
   }
   if (n == "walk_layout") {
     *value = h->opt_layout;
-    return HBTU_OK;
-  }
-  if (n == "walk_stage_depth") {
-    *value = h->opt_stage;
     return HBTU_OK;
   }
   if (n == "small_cutoff") {

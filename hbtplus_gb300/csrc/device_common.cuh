@@ -30,12 +30,6 @@ __device__ __forceinline__ void load_node(const WNode *nd, int i, float4 &p, int
       : "l"(nd + i));
 }
 
-__device__ __forceinline__ void load_node_shared(const WNode *nd, int i, float4 &p, int4 &m)
-{
-  p = nd[i].p;
-  m = nd[i].m;
-}
-
 __device__ __forceinline__ void load_node(const WNode *nd, int i, float4 &p, int2 &m)
 {
   int4 q;
@@ -186,10 +180,6 @@ struct Ctx {
   long long *X2;
   void *scan_tmp2;
   int opt_layout;  // 1: the FP32 lane walk uses nd2
-  // 1..4: nd2 holds the nodes of depth <= stage_depth first (from the root
-  // down, each cell's children together) and the lane walk serves them from
-  // shared memory; 0: plain preorder of the blocks
-  int stage_depth;
   // partition
   long long *pcode, *pX;
   int *Pk, *Qk;
@@ -216,10 +206,6 @@ void launch_sibling_layout(Ctx &c, const PassPlan &pl);
 // faster walk pays for the extra pass over the nodes (the small trees of
 // correction passes do not).
 constexpr int kSiblingMinTree = 1 << 16;
-// Shared-memory staging of the top of each tree (option walk_stage_depth): at
-// most 1 + 8 + ... + 8^D node slots, 32 bytes each.
-constexpr int kStageMaxDepth = 4;
-inline int stage_slots(int depth) { return depth > 0 ? ((1 << (3 * (depth + 1))) - 1) / 7 : 0; }
 inline bool sibling_walk(const Ctx &c, const PassPlan &pl)
 {
   return c.P.precision != HBTU_PRECISION_FP64 && c.opt_schedule == 0 && c.opt_layout && c.nd2 &&

@@ -23,7 +23,6 @@ struct hbtu_handle {
   int64_t opt_leaf_runs = 1;
   int64_t opt_schedule = 0;
   int64_t opt_layout = 1;
-  int64_t opt_stage = 0;
   int64_t opt_small = hbtu::kSmallDefault;
   int64_t opt_small_per_sm = 1;
   std::vector<cudaEvent_t> events;  // pool: 4 per pass when timing, 2 per call

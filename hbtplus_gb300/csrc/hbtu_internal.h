@@ -62,7 +62,6 @@ struct SegState {
   int t0, ntree, ntgt;
   float mfac;
   int nnodes;
-  int ntop;             // sibling-block slots from the root that the walk stages (0: none)
   int tgt_mode;         // 0 tree leaves (Morton), 1 last full pass's order, 2 list order
   int coh_n;            // length of that Morton order
   int ub_lo, ub_hi;     // list block removed by the last partition, to be sorted

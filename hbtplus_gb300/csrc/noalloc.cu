@@ -148,7 +148,6 @@ extern "C" hbtu_status hbtu_unbind_noalloc(const hbtu_params *params, const hbtu
     c.opt_leaf_runs = 1;
     c.opt_schedule = 0;
     c.opt_layout = 0;
-    c.stage_depth = 0;
     c.small_cap = 0;  // every pass on the batch kernels
     c.small_per_sm = 1;
     SegState g;

@@ -332,10 +332,7 @@ __global__ void __launch_bounds__(kTB) k_sib_count(Ctx c, int ntotal)
   } else {  // a bucket: its particles follow it, one after another
     k = end - idx - 1;
   }
-  // blocks of the staged top (children of cells above the stage depth) are
-  // counted in the high half, the rest in the low half: one scan places both
-  const bool top = c.cdepth[e] < c.stage_depth;
-  c.X2[idx] = top ? (long long)k << 32 : (long long)k;
+  c.X2[idx] = k;
 }
 
 // the slots of every cell's children: its block starts after the blocks of
@@ -348,15 +345,8 @@ __global__ void __launch_bounds__(kTB) k_sib_assign(Ctx c, int ntotal)
   const int s = c.sb.hi_a[e];
   const int root = 2 * c.tree_base[s];
   const int idx = c.cidx[e], end = c.cskip[e];
-  const long long before = c.X2[idx] - c.X2[root];
-  const long long all = c.X2[root + c.seg[s].nnodes] - c.X2[root];
-  const int ntop = (int)(all >> 32);  // slots of the staged blocks
-  const bool top = c.cdepth[e] < c.stage_depth;
-  const int base = root + 1 + (top ? (int)(before >> 32) : ntop + (int)(before & 0xffffffffLL));
-  if (idx == root) {
-    c.newidx[root] = root;
-    c.seg[s].ntop = c.stage_depth > 0 ? 1 + ntop : 0;
-  }
+  const int base = root + 1 + (int)(c.X2[idx] - c.X2[root]);
+  if (idx == root) c.newidx[root] = root;
   int k = 0;
   if (c.cdepth[e] < c.seg[s].levels) {
     for (int j = 0; j < 8; j++) {
@@ -379,7 +369,6 @@ __global__ void k_sib_single(Ctx c)
   const int root = 2 * c.tree_base[s];
   c.newidx[root] = root;
   c.newidx[root + 1] = root + 1;
-  c.seg[s].ntop = 0;
 }
 
 // every live node slot: its record at its new slot, pointers renumbered

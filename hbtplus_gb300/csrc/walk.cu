@@ -171,68 +171,6 @@ __global__ void __launch_bounds__(kB) k_walk_fp32_lean(Ctx c, int total)
   count_interactions(c, t.s, ninter);
 }
 
-// The same walk with the top of the tree in shared memory: when every target
-// of the block walks one tree, the block copies that tree's first ntop slots
-// (the nodes down to the stage depth, placed first by the sibling-block
-// layout) and reads them there; a block whose targets span several trees
-// reads every node from global memory.  The nodes visited, their order and
-// the arithmetic are those of k_walk_fp32_lean.
-template <int kB>
-__global__ void __launch_bounds__(kB) k_walk_fp32_staged(Ctx c, int total, int cap)
-{
-  HBTU_KERNEL_PROLOGUE();
-  extern __shared__ WNode top[];
-  __shared__ int s_lo, s_hi, s_cnt;
-  Target t;
-  load_target<true>(c, blockIdx.x * kB + threadIdx.x, total, t);
-  if (threadIdx.x == 0) {
-    s_lo = kDone;
-    s_hi = -1;
-    s_cnt = 0;
-  }
-  __syncthreads();
-  const bool walks = t.nxt != kDone && t.nxt < t.end;
-  const int lo = __reduce_min_sync(0xffffffffu, walks ? t.nxt : kDone);
-  const int hi = __reduce_max_sync(0xffffffffu, walks ? t.nxt : -1);
-  if ((threadIdx.x & 31) == 0) {
-    atomicMin(&s_lo, lo);
-    atomicMax(&s_hi, hi);
-  }
-  __syncthreads();
-  const int root = s_lo;
-  if (walks && root == s_hi)  // one tree: every walking lane writes the same count
-    s_cnt = min(min(c.seg[t.s].ntop, t.end - root), cap);
-  __syncthreads();
-  const int ntop = s_cnt;
-  for (int i = threadIdx.x; i < ntop; i += kB) top[i] = c.nd2[root + i];
-  __syncthreads();
-  int ninter = 0;
-  const double pot = walk_lean<true, true>(c.nd2, t, c.P, &ninter, top, ntop);
-  finish_target(c, t, pot);
-  count_interactions(c, t.s, ninter);
-}
-
-template <int kB>
-void launch_staged_kb(Ctx &c, int n)
-{
-  const int cap = stage_slots(c.stage_depth);
-  const size_t smem = sizeof(WNode) * (size_t)cap;
-  if (smem > 48 * 1024)
-    HBTU_CUDA(cudaFuncSetAttribute(k_walk_fp32_staged<kB>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  launch_k(k_walk_fp32_staged<kB>, (n + kB - 1) / kB, kB, smem, c.st, c, n, cap);
-}
-
-void launch_staged(Ctx &c, int n)
-{
-  if (n >= 152 * 4 * 512)
-    launch_staged_kb<512>(c, n);
-  else if (n >= 152 * 4 * 256)
-    launch_staged_kb<256>(c, n);
-  else
-    launch_staged_kb<128>(c, n);
-}
-
 template <bool kSib>
 void launch_lean(Ctx &c, int n)
 {
@@ -404,8 +342,6 @@ void launch_walk(Ctx &c, const PassPlan &pl)
     launch_k(k_walk_fp32<true>, blocks, kWB, 0, c.st, c, n);
   else if (c.opt_schedule == 1)
     launch_k(k_walk_fp32<false>, blocks, kWB, 0, c.st, c, n);
-  else if (sibling_walk(c, pl) && c.stage_depth > 0)  // top slots placed first
-    launch_staged(c, n);
   else if (sibling_walk(c, pl))  // the tree build made the sibling-block records
     launch_lean<true>(c, n);
   else

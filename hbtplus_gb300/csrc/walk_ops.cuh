@@ -199,12 +199,9 @@ static __device__ __noinline__ bool exact_open(float4 na, float qx, float qy, fl
 // the interactions.
 constexpr float kBandRatio = 1.0000200002f;  // (1 + 1e-5) / (1 - 1e-5), rounded up
 
-// kStage: the first `ntop` slots from the target's root are also in shared
-// memory (`top`), and the walk reads them there.
-template <bool kSib, bool kStage = false>
+template <bool kSib>
 __device__ __forceinline__ double walk_lean(const WNode *nodes, const Target &t,
-                                            const DevParams &P, int *ninter,
-                                            const WNode *top = nullptr, int ntop = 0)
+                                            const DevParams &P, int *ninter)
 {
   const float hf = (float)P.h, hinvf = (float)P.h_inv, h2f = hf * hf;
   const double th2d = (double)P.theta2;
@@ -216,10 +213,7 @@ __device__ __forceinline__ double walk_lean(const WNode *nodes, const Target &t,
   while (cur < end) {
     float4 na;
     int4 nm;
-    if (kStage && (unsigned)(cur - t.nxt) < (unsigned)ntop)
-      load_node_shared(top, cur - t.nxt, na, nm);
-    else
-      load_node(nodes, cur, na, nm);
+    load_node(nodes, cur, na, nm);
     const float r2 = dist2(na, t.q);
     const float lo = __int_as_float(nm.z);
     const float up = kSib ? lo * kBandRatio : __int_as_float(nm.w);

@@ -4,25 +4,18 @@ visits the same nodes in the same order as the walk over the preorder
 records (walk_layout 0), so every output of the unbinding is the same bit
 for bit: orders, energies, results, interaction counts.  Batches with
 subhaloes on box faces, a large single subhalo at two opening angles, and
-the energies-only entry (hbtu_binding_energies) with potentials.
-
-The same holds with the top of each tree staged in shared memory (option
-walk_stage_depth 1..4): the layout then places the nodes down to that depth
-first and the walk reads them from shared memory, visiting the same nodes in
-the same order."""
+the energies-only entry (hbtu_binding_energies) with potentials."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 
-def run(params, batch, layout, precision=0, stage=0):
+def run(params, batch, layout, precision=0):
     from hbtplus_gb300.unbind import Unbinder
     with Unbinder(params, precision=precision) as ub:
         ub.set_option("walk_layout", layout)
         assert ub.get_option("walk_layout") == layout
-        ub.set_option("walk_stage_depth", stage)
-        assert ub.get_option("walk_stage_depth") == stage
         return ub.unbind_batch(batch, check_status=False)
 
 
@@ -65,25 +58,3 @@ def test_binding_energies_layouts_agree():
             out.append(ub.binding_energies(sub["pos"], sub["vel"], sub["mass"], sub["ref_pos"],
                                            sub["ref_vel"]))
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
-
-
-@pytest.mark.parametrize("depth", [1, 2, 3, 4])
-def test_staged_top_agrees(depth):
-    from hbtplus_gb300 import synthetic as S
-    b = S.subhalo_batch(nsub=1200, seed=75)
-    p = S.default_params()
-    same(run(p, b, 1, stage=depth), run(p, b, 1))
-
-
-def test_staged_top_single_subhalo_and_limits():
-    from hbtplus_gb300 import synthetic as S
-    from hbtplus_gb300.unbind import Unbinder
-    b = S.concat([S.single_subhalo(n=200_000, seed=76)])
-    p = S.default_params(open_angle=0.45)
-    ref = run(p, b, 1)
-    for depth in (3, 4):
-        same(run(p, b, 1, stage=depth), ref)
-    with Unbinder(p) as ub:
-        for bad in (-1, 5):
-            with pytest.raises(Exception):
-                ub.set_option("walk_stage_depth", bad)
