@@ -77,8 +77,6 @@ static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S, boo
   c.sb.os_ghist = cv.take<unsigned>(16 * 256);
   c.sb.os_goff = cv.take<unsigned>(16 * 256);
   c.scan_tmp = cv.take<char>(scan_tmp_bytes(N + 1));
-  c.childL = cv.take<int>(N);
-  c.childR = cv.take<int>(N);
   c.parentI = cv.take<int>(N);
   c.parentL = cv.take<int>(N);
   c.rfirst = cv.take<int>(N);
@@ -92,6 +90,7 @@ static void carve(Carver &cv, Ctx &c, Staging &sg, long long N, long long S, boo
   c.pending0 = cv.take<int>(N);
   c.cslot = cv.take<int>(8 * N);
   c.cell_list = cv.take<int>(N);
+  c.chunk_list = cv.take<int>(N);
   c.lvl = cv.take<int>(96);
   c.pending = cv.take<int>(N);
   c.mask = cv.take<unsigned long long>(N);

@@ -106,9 +106,18 @@ __device__ __forceinline__ float vdot(const float a[3], const float b[3])
 }
 
 // Relative coordinate of an absolute float coordinate: wrapped once in
-// double, then rounded to float.
+// double, then rounded to float.  When the float difference s = x - c is
+// exact (a float TwoSum with a zero error term) it equals the double one, and
+// for |s| < box the wrap s -+ box is exact in float as in double (Sterbenz:
+// box/2 < |s| < 2 box), so the float arithmetic gives the same bits without
+// the FP64 pipe (1/64 of the FP32 rate on this GPU); otherwise the double path.
 __device__ __forceinline__ float rel_coord(float x, float c, const DevParams &P)
 {
+  const float s = __fsub_rn(x, c);
+  const float bb = __fsub_rn(s, x);
+  const float err = __fadd_rn(__fsub_rn(x, __fsub_rn(s, bb)), __fsub_rn(-c, bb));
+  if (err == 0.f && !P.periodic) return s;
+  if (err == 0.f && fabsf(s) < P.box) return nearest_f(s, P);
   double d = dsub(f2d(x), f2d(c));
   if (P.periodic) d = nearest_d(d, P);
   return d2f(d);
@@ -163,10 +172,13 @@ struct Ctx {
   // sort
   SortBuffers sb;
   // tree construction
-  int *childL, *childR, *parentI, *parentL, *rfirst, *rlast, *dnode;
+  int *parentI, *parentL, *rfirst, *rlast, *dnode;
   int *iscell, *cidx, *cskip, *cdepth, *pcell, *pending, *pending0;  // pending: child cells
   int *cslot;  // 8 per cell: node index of the child in each octant, -1 if none
-  int *cell_list, *lvl;  // cells grouped by octal depth; per-depth counts, starts, cursors
+  // moment work lists: cell_list holds the large chunk roots from the front and
+  // the top cells from the back, chunk_list the small chunk roots; lvl[0..3]:
+  // their counts (large, top), the job counter, the small count
+  int *cell_list, *chunk_list, *lvl;
   unsigned long long *mask;
   long long *X;
   // nodes (2 per tree particle)

@@ -20,14 +20,30 @@
 //      pointer that leaves the tree is stored as kDone);
 //   6. bottom-up mass and centre of mass over each cell's children in octant
 //      order, in double, rounded to float per cell as the reference does
-//      (ProcessNode / FillNodeCenter, src/gravity_tree.cpp:18-46).
+//      (ProcessNode / FillNodeCenter, src/gravity_tree.cpp:18-46): one
+//      thread block per subtree of at most kChunkKeys particles, depth by
+//      depth between block barriers, then an atomic-countdown climb over the
+//      few cells above those subtrees.
+#include <algorithm>
+
 #include "tree_ops.cuh"
 
 namespace hbtu {
 namespace {
 
 constexpr int kTB = 256;
-constexpr int kLevelSyncMin = 1 << 18;  // tree particles from which moments go level by level
+// Moments: a cell whose subtree holds at most kChunkKeys particles and whose
+// parent's holds more (or that is a root) is a chunk root; a block computes
+// the cells of kBatch chunks at a time.  Cells above the chunk roots are top
+// cells.
+constexpr int kChunkKeys = 2048;
+constexpr int kChunkThreads = 256;
+// Chunks of more than kSmallChunkKeys particles are computed one per block,
+// the others kBatch at a time, so that a block's work stays within 2x of
+// another's.
+constexpr int kSmallChunkKeys = 256;
+constexpr int kBatch = 16;
+constexpr int kDepthBins = 32;  // octal depths 0 .. kMaxLevels
 
 __global__ void __launch_bounds__(kTB) k_bbox_chunks(Ctx c)
 {
@@ -160,80 +176,211 @@ __global__ void __launch_bounds__(kTB) k_cellnodes(Ctx c, int ntotal)
   const int s = c.sb.hi_a[e];
   const int base = c.tree_base[s], n = c.tree_base[s + 1] - base;
   cellnodes_elem(c, c.seg[s], base, n, e, c.sb.lo_a + base, c.X + base);
+  // moment work lists: large chunk roots at the front of cell_list (count
+  // lvl[0]), top cells at its back (count lvl[1]), small chunk roots in
+  // chunk_list (count lvl[3]).  pending0 of a top cell counts its top child
+  // cells twice over: in the high half (kept) and in the low half (counted
+  // down by the climb).
+  const int p = c.pcell[e];
+  const int keys = c.rlast[e] - c.rfirst[e] + 1;
+  if (keys > kChunkKeys) {
+    if (p >= 0) atomicAdd(&c.pending0[p], 0x10001);
+    c.cell_list[ntotal - 1 - atomicAdd(&c.lvl[1], 1)] = e;
+  } else if (p < 0 || c.rlast[p] - c.rfirst[p] + 1 > kChunkKeys) {
+    if (keys > kSmallChunkKeys)
+      c.cell_list[atomicAdd(&c.lvl[0], 1)] = e;
+    else
+      c.chunk_list[atomicAdd(&c.lvl[3], 1)] = e;
+  }
 }
 
-// Bottom-up moments (cell_moment): a cell is summed once all its child cells
-// are, by the thread that finished the last child (atomic countdown, no
-// waiting).  A cell without child cells is marked for the walk's leaf runs
-// (sign bit of len*len).
-__global__ void __launch_bounds__(kTB) k_moments(Ctx c, int ntotal)
+// A cell of a moment step: its slot, skip, octant slots, subhalo frame centre.
+struct MomCell {
+  int idx, end;
+  bool bucket, mark;
+  int4 s0, s1;
+  float fc[3];
+};
+
+// Moments of the chunks.  The double arithmetic of a cell issues per warp
+// instruction whatever the number of active lanes, at 1/64 of the FP32 rate on
+// this GPU, so the cells computed together must fill the lanes: a persistent
+// block takes kBatch chunk roots at a time and aligns their subtrees at the
+// bottom, so that step t computes, in every chunk, the cells t levels above
+// its deepest ones, all of them spread over the block's threads, with one
+// barrier per step (every cell's child cells are deeper, so done before it).
+// The internal nodes of the Karras subtree over keys [first, last] rooted at
+// node i are nodes first..last-1 when i == first, first+1..last when i == last;
+// a warp lists the octree cells among them by depth in the chunk's own element
+// range of a scratch array (chunks' ranges are disjoint).  A cell without
+// child cells is marked for the walk's leaf runs (sign bit of len*len).
+__global__ void __launch_bounds__(kChunkThreads) k_moments_chunks(Ctx c)
 {
   HBTU_KERNEL_PROLOGUE();
-  int e = blockIdx.x * kTB + threadIdx.x;
-  if (e >= ntotal || !c.iscell[e] || c.pending0[e] != 0) return;
-  c.nd[c.cidx[e]].m.x |= (int)0x80000000;
-  for (int level = 0; level <= 2 * kMaxLevels + 2; level++) {
-    const int s = c.sb.hi_a[e];
-    cell_moment<true>(c, c.seg[s], e, c.cdepth[e]);
-    __threadfence();
+  constexpr unsigned kFull = 0xffffffffu;
+  constexpr int kWarps = kChunkThreads / 32;
+  __shared__ int s_first, s_steps;
+  __shared__ int s_lo[kBatch], s_maxd[kBatch], s_pre[kDepthBins][kBatch + 1];
+  __shared__ int s_cnt[kBatch][kDepthBins], s_start[kBatch][kDepthBins];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int *glist = reinterpret_cast<int *>(c.X);  // the cell-slot scan is no longer needed
+  const int nlarge = c.lvl[0], nsmall = c.lvl[3];
+  const int njobs = nlarge + (nsmall + kBatch - 1) / kBatch;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_first = atomicAdd(&c.lvl[2], 1);  // a large chunk, or a batch of small ones
+      s_steps = 0;
+    }
+    __syncthreads();
+    const int job = s_first;
+    if (job >= njobs) return;
+    const int *roots = job < nlarge ? c.cell_list + job : c.chunk_list + (job - nlarge) * kBatch;
+    const int nb = job < nlarge ? 1 : min(kBatch, nsmall - (job - nlarge) * kBatch);
+    // each warp lists the cells of its chunks by depth below the chunk root
+    for (int j = w; j < nb; j += kWarps) {
+      int *cnt = s_cnt[j], *start = s_start[j];
+      const int e0 = roots[j];
+      const int base = c.tree_base[c.sb.hi_a[e0]];
+      const int first = c.rfirst[e0], last = c.rlast[e0];
+      const int lo = base + (e0 - base == first ? first : first + 1);
+      const int nint = last - first;  // internal nodes of the subtree
+      const int d0 = c.cdepth[e0];
+      cnt[lane] = 0;
+      __syncwarp();
+      int maxd = 0;
+      for (int k = lane; k < nint; k += 32) {
+        const int d = c.cdepth[lo + k];  // -1: not a cell
+        if (d >= 0) {
+          const int r = min(max(d - d0, 0), kDepthBins - 1);
+          atomicAdd(&cnt[r], 1);
+          maxd = max(maxd, r);
+        }
+      }
+      maxd = __reduce_max_sync(kFull, maxd);
+      __syncwarp();
+      const int v = cnt[lane];
+      int incl = v;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+      }
+      start[lane] = lo + incl - v;
+      cnt[lane] = 0;
+      __syncwarp();
+      for (int k = lane; k < nint; k += 32) {
+        const int e = lo + k;
+        const int d = c.cdepth[e];
+        if (d >= 0) {
+          const int r = min(max(d - d0, 0), kDepthBins - 1);
+          glist[start[r] + atomicAdd(&cnt[r], 1)] = e;
+        }
+      }
+      if (lane == 0) {
+        s_lo[j] = lo;
+        s_maxd[j] = maxd;
+        atomicMax(&s_steps, maxd + 1);
+      }
+    }
+    __syncthreads();
+    const int steps = s_steps;
+    if (w == 0) {  // per step: where each chunk's cells start in the step's list
+      for (int t = 0; t < steps; t++) {
+        int v = 0;
+        if (lane < nb) {
+          const int r = s_maxd[lane] - t;
+          v = r >= 0 ? s_cnt[lane][r] : 0;
+        }
+        int incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int u = __shfl_up_sync(kFull, incl, o);
+          if (lane >= o) incl += u;
+        }
+        if (lane < kBatch) s_pre[t][lane + 1] = incl;
+        if (lane == 0) s_pre[t][0] = 0;
+      }
+    }
+    __syncthreads();
+    // A cell's records (slots, children's slots, subhalo) do not depend on the
+    // cells below it: each thread loads those of its next step's first cell
+    // before computing this step's, so a step waits only for the children's
+    // moments.
+    auto load_cell = [&](int t, int i, MomCell &q) {
+      const int *pre = s_pre[t];
+      int j = 0;  // the chunk: pre[j] <= i < pre[j + 1]
+#pragma unroll
+      for (int step = kBatch / 2; step > 0; step >>= 1)
+        if (j + step < nb && pre[j + step] <= i) j += step;
+      const int e = glist[s_start[j][s_maxd[j] - t] + (i - pre[j])];
+      const SegState &sg = c.seg[c.sb.hi_a[e]];
+      q.idx = c.cidx[e];
+      q.end = c.cskip[e];
+      q.bucket = c.cdepth[e] >= sg.levels;
+      q.mark = c.pending[e] == 0;
+      const int4 *slot = reinterpret_cast<const int4 *>(c.cslot + 8 * e);
+      q.s0 = slot[0];
+      q.s1 = slot[1];
+      q.fc[0] = sg.fc[0];
+      q.fc[1] = sg.fc[1];
+      q.fc[2] = sg.fc[2];
+    };
+    auto do_cell = [&](const MomCell &q) {
+      if (q.mark) c.nd[q.idx].m.x |= (int)0x80000000;
+      const float4 m = cell_moment_slots(q.bucket, q.idx, q.end, q.s0, q.s1,
+                                         [&](int k2) { return c.nd_abs[k2]; });
+      c.nd_abs[q.idx] = m;
+      store_cell_rel(c, q.fc, q.idx, m);
+    };
+    MomCell cur;
+    bool have = threadIdx.x < s_pre[0][nb];
+    if (have) load_cell(0, threadIdx.x, cur);
+    for (int t = 0; t < steps; t++) {
+      MomCell nxt;
+      const bool have_next = t + 1 < steps && (int)threadIdx.x < s_pre[t + 1][nb];
+      if (have_next) load_cell(t + 1, threadIdx.x, nxt);
+      if (have) do_cell(cur);
+      for (int i = threadIdx.x + kChunkThreads; i < s_pre[t][nb]; i += kChunkThreads) {
+        MomCell q;
+        load_cell(t, i, q);
+        do_cell(q);
+      }
+      __syncthreads();
+      cur = nxt;
+      have = have_next;
+    }
+  }
+}
+
+// Atomic add with acquire-release ordering at device scope: the adder's
+// earlier writes are visible to whoever reads the counter's new value.
+__device__ __forceinline__ int atomic_add_acq_rel(int *p, int v)
+{
+  int old;
+  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;"
+               : "=r"(old)
+               : "l"(p), "r"(v)
+               : "memory");
+  return old;
+}
+
+// Moments of the top cells (above the chunk roots, few): a cell is summed
+// once all its top child cells are, by the thread that finished the last one
+// (atomic countdown on the low half of pending0; the high half, never
+// changed, says whether the cell waits for any).  Children written during this
+// launch are read through L2.
+__global__ void __launch_bounds__(kTB) k_moments_top(Ctx c, int ntotal)
+{
+  HBTU_KERNEL_PROLOGUE();
+  const int i = blockIdx.x * kTB + threadIdx.x;
+  if (i >= c.lvl[1]) return;
+  int e = c.cell_list[ntotal - 1 - i];
+  if ((c.pending0[e] >> 16) != 0) return;  // a child's climb computes it
+  for (int guard = 0; guard <= 2 * kMaxLevels + 2; guard++) {
+    if (c.pending[e] == 0) c.nd[c.cidx[e]].m.x |= (int)0x80000000;
+    cell_moment<true>(c, c.seg[c.sb.hi_a[e]], e, c.cdepth[e]);
     const int p = c.pcell[e];
     if (p < 0) break;
-    if (atomicSub(&c.pending[p], 1) != 1) break;
-    __threadfence();
+    if ((atomic_add_acq_rel(&c.pending0[p], -1) & 0xffff) != 1) break;
     e = p;
-  }
-}
-
-// Large trees: the same moments one octal depth at a time, deepest first,
-// over a dense list of the cells of each depth, so a warp's 32 lanes work on
-// 32 cells (double arithmetic issues per warp instruction whatever the number
-// of active lanes, and runs at 1/64 of the FP32 rate on this GPU).
-constexpr int kDepthBins = 32;  // octal depths 0 .. kMaxLevels
-
-__global__ void __launch_bounds__(kTB) k_depth_count(Ctx c, int ntotal)
-{
-  HBTU_KERNEL_PROLOGUE();
-  __shared__ int h[kDepthBins];
-  if (threadIdx.x < kDepthBins) h[threadIdx.x] = 0;
-  __syncthreads();
-  const int e = blockIdx.x * kTB + threadIdx.x;
-  if (e < ntotal && c.cdepth[e] >= 0) atomicAdd(&h[c.cdepth[e]], 1);
-  __syncthreads();
-  if (threadIdx.x < kDepthBins && h[threadIdx.x]) atomicAdd(&c.lvl[threadIdx.x], h[threadIdx.x]);
-}
-
-// lvl[0..31] counts per depth, lvl[32..63] list start per depth, lvl[64..95] cursors
-__global__ void __launch_bounds__(kTB) k_depth_fill(Ctx c, int ntotal)
-{
-  HBTU_KERNEL_PROLOGUE();
-  __shared__ int h[kDepthBins], start[kDepthBins];
-  if (threadIdx.x < kDepthBins) h[threadIdx.x] = 0;
-  __syncthreads();
-  const int e = blockIdx.x * kTB + threadIdx.x;
-  const int d = e < ntotal ? c.cdepth[e] : -1;
-  int rank = 0;
-  if (d >= 0) rank = atomicAdd(&h[d], 1);
-  __syncthreads();
-  if (threadIdx.x < kDepthBins) {
-    int off = 0;
-    for (int k = 0; k < (int)threadIdx.x; k++) off += c.lvl[k];
-    if (blockIdx.x == 0) c.lvl[kDepthBins + threadIdx.x] = off;
-    start[threadIdx.x] = h[threadIdx.x] ? off + atomicAdd(&c.lvl[2 * kDepthBins + threadIdx.x],
-                                                          h[threadIdx.x])
-                                        : 0;
-  }
-  __syncthreads();
-  if (d >= 0) c.cell_list[start[d] + rank] = e;
-}
-
-__global__ void __launch_bounds__(kTB) k_moments_level(Ctx c, int depth)
-{
-  HBTU_KERNEL_PROLOGUE();
-  const int count = c.lvl[depth], first = c.lvl[kDepthBins + depth];
-  for (int i = blockIdx.x * kTB + threadIdx.x; i < count; i += gridDim.x * kTB) {
-    const int e = c.cell_list[first + i];
-    if (c.pending[e] == 0) c.nd[c.cidx[e]].m.x |= (int)0x80000000;
-    cell_moment<false>(c, c.seg[c.sb.hi_a[e]], e, depth);
   }
 }
 
@@ -272,6 +419,8 @@ void launch_tree_build(Ctx &c, const PassPlan &pl)
   radix_sort(c.sb, n, words, shifts, np, c.st);
   HBTU_CUDA(cudaMemsetAsync(c.mask, 0, sizeof(unsigned long long) * (size_t)n, c.st));
   HBTU_CUDA(cudaMemsetAsync(c.pending, 0, sizeof(int) * (size_t)n, c.st));
+  HBTU_CUDA(cudaMemsetAsync(c.pending0, 0, sizeof(int) * (size_t)n, c.st));
+  HBTU_CUDA(cudaMemsetAsync(c.lvl, 0, sizeof(int) * 4, c.st));
   HBTU_CUDA(cudaMemsetAsync(c.cslot, 0xff, sizeof(int) * 8 * (size_t)n, c.st));
   launch_k(k_karras, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
@@ -284,22 +433,19 @@ void launch_tree_build(Ctx &c, const PassPlan &pl)
   HBTU_LAUNCHED();
   launch_k(k_cellnodes, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
-  if (n < kLevelSyncMin) {  // small trees: one launch, climbing by atomic countdown
-    HBTU_CUDA(cudaMemcpyAsync(c.pending0, c.pending, sizeof(int) * (size_t)n,
-                              cudaMemcpyDeviceToDevice, c.st));
-    launch_k(k_moments, nblk(n), kTB, 0, c.st, c, n);
-    HBTU_LAUNCHED();
-  } else {  // large trees: dense per-depth cell lists, one launch per depth
-    HBTU_CUDA(cudaMemsetAsync(c.lvl, 0, sizeof(int) * 3 * kDepthBins, c.st));
-    launch_k(k_depth_count, nblk(n), kTB, 0, c.st, c, n);
-    HBTU_LAUNCHED();
-    launch_k(k_depth_fill, nblk(n), kTB, 0, c.st, c, n);
-    HBTU_LAUNCHED();
-    for (int d = pl.max_levels; d >= 0; d--) {
-      launch_k(k_moments_level, 152 * 2, kTB, 0, c.st, c, d);
-      HBTU_LAUNCHED();
-    }
-  }
+  int dev = 0, sms = 0, per_sm = 0;  // a persistent grid: the resident blocks
+  HBTU_CUDA(cudaGetDevice(&dev));
+  HBTU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  HBTU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_moments_chunks,
+                                                          kChunkThreads, 0));
+  const int njob_max = std::max(1, n / 2);  // a chunk root holds at least 2 particles
+  launch_k(k_moments_chunks, std::min(sms * std::max(per_sm, 1), njob_max), kChunkThreads, 0,
+           c.st, c);
+  HBTU_LAUNCHED();
+  // top cells hold more than kChunkKeys particles each, at most n / kChunkKeys per depth
+  const int ntop_max = std::max(1, (n / kChunkKeys) * (pl.max_levels + 1));
+  launch_k(k_moments_top, nblk(std::min(ntop_max, n)), kTB, 0, c.st, c, n);
+  HBTU_LAUNCHED();
   if (sibling_walk(c, pl)) launch_sibling_layout(c, pl);
 }
 

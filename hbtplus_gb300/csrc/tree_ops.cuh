@@ -170,8 +170,8 @@ __device__ __forceinline__ int kdelta(const unsigned long long *keys, int n, int
 }
 
 // Internal node i (0 <= i < n-1) of the Karras (2012) binary radix tree over
-// a subhalo's sorted keys.  Child codes: internal node -> its element index;
-// leaf -> ~element index.
+// a subhalo's sorted keys: its key range, split depth, and the parent links of
+// its two children (parentI for an internal child, parentL for a leaf).
 __device__ __forceinline__ void karras_elem(const Ctx &c, const unsigned long long *keys, int base,
                                             int n, int i)
 {
@@ -195,20 +195,14 @@ __device__ __forceinline__ void karras_elem(const Ctx &c, const unsigned long lo
   c.rfirst[e] = first;
   c.rlast[e] = last;
   c.dnode[e] = dn;
-  if (first == gamma) {
-    c.childL[e] = ~(base + gamma);
+  if (first == gamma)  // the left child is a leaf (key gamma) or internal node gamma
     c.parentL[base + gamma] = e;
-  } else {
-    c.childL[e] = base + gamma;
+  else
     c.parentI[base + gamma] = e;
-  }
-  if (last == gamma + 1) {
-    c.childR[e] = ~(base + gamma + 1);
+  if (last == gamma + 1)  // the right child: leaf or internal node gamma + 1
     c.parentL[base + gamma + 1] = e;
-  } else {
-    c.childR[e] = base + gamma + 1;
+  else
     c.parentI[base + gamma + 1] = e;
-  }
   if (i == 0) c.parentI[e] = -1;
 }
 
@@ -334,54 +328,114 @@ __device__ __forceinline__ void cellnodes_elem(const Ctx &c, const SegState &sg,
   }
 }
 
-// Bottom-up moments of one cell: mass and centre of mass over its children in
-// octant order, in double, rounded to float as the reference does.  The
-// children come from the cell's eight octant slots; a bucket cell (particles
-// sharing the whole key, depth == levels) walks its children by skip
-// pointers.  kCG: read the children's moments through L2 (.cg), for callers
-// whose children were written by other blocks during the same launch.
-// A product of two floats is exact in double, so one fused multiply-add
-// rounds exactly as the reference's multiply-then-add.
-template <bool kCG>
-__device__ __forceinline__ void add_child(const Ctx &c, int k, double &m, double &cx, double &cy,
-                                          double &cz)
+// 1/m to within a few units in the last place: the hardware's approximate
+// double reciprocal refined by two Newton-Raphson steps r <- r + r (1 - m r)
+// (each step squares the relative error).  ok: the residual 1 - m r, taken
+// once more, shows a relative error below 2^-49 (else r is not used).
+__device__ __forceinline__ double recip_refined(double m, bool &ok)
 {
-  const float4 a = kCG ? __ldcg(&c.nd_abs[k]) : c.nd_abs[k];
-  const double w = f2d(a.w);
-  m = dadd(m, w);
-  cx = __fma_rn(f2d(a.x), w, cx);
-  cy = __fma_rn(f2d(a.y), w, cy);
-  cz = __fma_rn(f2d(a.z), w, cz);
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(m));
+  r = __fma_rn(r, __fma_rn(-m, r, 1.0), r);
+  r = __fma_rn(r, __fma_rn(-m, r, 1.0), r);
+  ok = fabs(__fma_rn(-m, r, 1.0)) < 0x1p-49;
+  return r;
 }
 
+// float(c / m) with the quotient first rounded to double, as the reference
+// rounds its double centre of mass to float, given r ~ 1/m (ok as above).
+// q = c * r then lies within a few double units in the last place of the
+// correctly rounded quotient, so both round to the same float unless q lies
+// within 64 units of a point halfway between two floats (its low 29 mantissa
+// bits near 2^28), or outside the range of normal floats; those take the
+// exact division.
+__device__ __forceinline__ float quot_float(double c, double m, double r, bool ok)
+{
+  const double q = dmul(c, r);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(q);
+  const int ex = (int)((b >> 52) & 0x7ffull);
+  const unsigned rem = (unsigned)(b & 0x1fffffffull);
+  if (ok && ex >= 1023 - 125 && ex <= 1023 + 126 && rem - (0x10000000u - 64u) > 128u)
+    return d2f(q);
+  return d2f(ddiv(c, m));
+}
+
+// Bottom-up moments of one cell: mass and centre of mass over its children in
+// octant order, in double, rounded to float as the reference does.  The
+// children come from the cell's eight octant slots; the children of a bucket
+// cell (particles sharing the whole key, depth == levels) hold the slots that
+// follow it, in preorder, so they are read one after another.  src(k) gives
+// the moment {x, y, z, m} of node slot k (global memory, or a block's copy).
+// A product of two floats is exact in double, so one fused multiply-add
+// rounds exactly as the reference's multiply-then-add.
+// The same with the cell's octant slots s0, s1 (cslot) already loaded;
+// bucket: the cell is a bucket (depth == levels).
+template <class Src>
+__device__ __forceinline__ float4 cell_moment_slots(bool bucket, int idx, int end, int4 s0,
+                                                    int4 s1, Src src)
+{
+  double m = 0., cx = 0., cy = 0., cz = 0.;
+  auto add = [&](int k) {
+    const float4 a = src(k);
+    const double w = f2d(a.w);
+    m = dadd(m, w);
+    cx = __fma_rn(f2d(a.x), w, cx);
+    cy = __fma_rn(f2d(a.y), w, cy);
+    cz = __fma_rn(f2d(a.z), w, cz);
+  };
+  if (!bucket) {
+    const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (sl[j] > idx && sl[j] < end) add(sl[j]);
+  } else {
+#pragma unroll 4
+    for (int k = idx + 1; k < end; k++) add(k);
+  }
+  bool ok;
+  const double r = recip_refined(m, ok);
+  return make_float4(quot_float(cx, m, r, ok), quot_float(cy, m, r, ok), quot_float(cz, m, r, ok),
+                     d2f(m));
+}
+
+template <bool kCG, class Src>
+__device__ __forceinline__ float4 cell_moment_of(const Ctx &c, const SegState &sg, int e,
+                                                 int depth, int idx, int end, Src src)
+{
+  int4 s0 = make_int4(-1, -1, -1, -1), s1 = s0;
+  const bool bucket = depth >= sg.levels;
+  if (!bucket) {
+    const int4 *slot = reinterpret_cast<const int4 *>(c.cslot + 8 * e);
+    s0 = kCG ? __ldcg(slot) : slot[0];
+    s1 = kCG ? __ldcg(slot + 1) : slot[1];
+  }
+  return cell_moment_slots(bucket, idx, end, s0, s1, src);
+}
+
+// The walk record's position and mass of a cell from its moment (fc: the
+// subhalo's frame centre).
+__device__ __forceinline__ void store_cell_rel(const Ctx &c, const float fc[3], int idx, float4 r)
+{
+  float4 rel = make_rel(r, fc, c.P);
+  rel.w = -rel.w;  // the sign bit marks a cell for the walks
+  c.nd[idx].p = rel;
+}
+
+// cell_moment_of over the moments in global memory (kCG: through L2, for
+// callers whose children were written by other blocks during the same
+// launch); stores the cell's moment and record.
 template <bool kCG>
 __device__ __forceinline__ void cell_moment(const Ctx &c, const SegState &sg, int e, int depth)
 {
   const int idx = c.cidx[e], end = c.cskip[e];
-  double m = 0., cx = 0., cy = 0., cz = 0.;
-  if (depth < sg.levels) {
-    const int4 *slot = reinterpret_cast<const int4 *>(c.cslot + 8 * e);
-    const int4 s0 = kCG ? __ldcg(slot) : slot[0];
-    const int4 s1 = kCG ? __ldcg(slot + 1) : slot[1];
-    const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
-#pragma unroll
-    for (int j = 0; j < 8; j++)
-      if (sl[j] > idx && sl[j] < end) add_child<kCG>(c, sl[j], m, cx, cy, cz);
-  } else {
-    for (int k = idx + 1; k < end;) {
-      add_child<kCG>(c, k, m, cx, cy, cz);
-      const int nk = c.nd[k].m.y;
-      k = nk > k ? nk : end;  // skip pointers always move forward
-    }
-  }
-  const float4 r = make_float4(d2f(ddiv(cx, m)), d2f(ddiv(cy, m)), d2f(ddiv(cz, m)), d2f(m));
+  const float4 r = cell_moment_of<kCG>(c, sg, e, depth, idx, end, [&](int k) {
+    return kCG ? __ldcg(&c.nd_abs[k]) : c.nd_abs[k];
+  });
   if (kCG)
     __stcg(&c.nd_abs[idx], r);
   else
     c.nd_abs[idx] = r;
-  float4 rel = make_rel(r, sg.fc, c.P);
-  rel.w = -rel.w;  // the sign bit marks a cell for the walks
-  c.nd[idx].p = rel;
+  store_cell_rel(c, sg.fc, idx, r);
 }
 
 }  // namespace hbtu

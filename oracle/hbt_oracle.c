@@ -179,6 +179,11 @@ static void update_internal(otree *t, int64_t no, int64_t sib, double len, const
   for (int k = 0; k < 3; k++) t->s[c][k] = (float)(com[k] / mass);
 }
 
+/* drand48 draws of the calling thread's current subhalo (one subhalo runs on
+ * one thread): reported per subhalo, since a process-global stream shared by
+ * threads makes those splits depend on thread timing. */
+static _Thread_local int64_t random_splits;
+
 /* OctTree_t::Build, src/oct_tree.tpp:16-144, followed by UpdateInternalNodes. */
 static void tree_build(otree *t, const int64_t *pid, int64_t np, const float *pos,
                        const float *mass, float mass_factor, const dpar *d)
@@ -242,6 +247,7 @@ static void tree_build(otree *t, const int64_t *pid, int64_t np, const float *po
         nodeid = newnodeid;
         if (lenhalf < d->reshalf) {
           /* particles closer than the resolution: random octant (tpp:112-123) */
+          random_splits++;
           sub = (int64_t)(8.0 * drand48());
           if (sub >= 8) sub = 7;
         } else {
@@ -621,6 +627,7 @@ static int unbind_one(const dpar *d, int64_t n, const int64_t *id, const float *
                       int nthr)
 {
   memset(res, 0, sizeof(*res));
+  random_splits = 0;
   memcpy(res->ref_pos, st->ref_pos, sizeof(res->ref_pos));
   memcpy(res->ref_vel, st->ref_vel, sizeof(res->ref_vel));
   memcpy(res->mostbound_pos, st->mostbound_pos, sizeof(res->mostbound_pos));
@@ -770,6 +777,7 @@ static int unbind_one(const dpar *d, int64_t n, const int64_t *id, const float *
   tree_free(&tree);
   free(E);
   free(pid);
+  res->random_splits = random_splits;
   return rc;
 }
 

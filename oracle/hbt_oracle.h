@@ -66,6 +66,7 @@ typedef struct hbto_result {
   int32_t too_few;                /* 1 if n < MinNumPartOfSub (death is recorded) */
   int64_t evaluations;            /* target potentials evaluated, all passes */
   int64_t interactions;           /* walk contributions summed, all passes */
+  int64_t random_splits;          /* sub-resolution cells split at random (drand48), all passes */
 } hbto_result;
 
 /* Unbind one subhalo.

@@ -70,6 +70,7 @@ class Result(C.Structure):
         ("too_few", C.c_int32),
         ("evaluations", C.c_int64),
         ("interactions", C.c_int64),
+        ("random_splits", C.c_int64),
     ]
 
 

@@ -12,24 +12,30 @@ Two settings of MaxSampleSizeOfPotentialEstimate:
         the tree is built over a 1000-particle sample with scaled masses and
         RefineBindingEnergyOrder reorders the first 1000 bound particles.
 
+Cells below TreeNodeResolution are split by the reference into random
+octants with its process-global drand48 stream (src/oct_tree.tpp:112-123) and
+kept whole here.  The oracle counts those draws per subhalo (random_splits);
+with the batch unbound on many threads, which numbers a subhalo draws depends
+on thread timing, so such a subhalo's reference tree changes from run to run.
+
 Tolerances:
   FP32 mode: a particle may change side only if its energy lies in the band
     |E| <= 1e-5 * max|E_bound|; Mbound within 1e-5 relative plus one particle
     mass per changed particle; bound energies within 2e-6 * max|E_bound|
-    (subhaloes where no particle changed side); iteration counts exact;
-    interaction counts within 1e-6 relative (the walk takes the reference's
-    opening decision in double near the threshold, but on float coordinates
-    relative to the frame, which are exact except across a periodic face when
-    one side lies close to 0: a decision within ~1e-7 of the threshold can
-    then flip); the same most-bound particle unless the reference's two
-    lowest energies lie within 2e-6 * max|E_bound| of each other.
+    (subhaloes where no particle changed side; 1e-5 where the reference split
+    a cell at random); iteration counts exact; interaction counts within 1e-6
+    relative (the walk takes the reference's opening decision in double near
+    the threshold, but on float coordinates relative to the frame, which are
+    exact except near the frame's origin: a decision within ~1e-7 of the
+    threshold can then flip; 1e-5 where the reference split a cell at
+    random); the same most-bound particle unless the reference's two lowest
+    energies lie within 2e-6 * max|E_bound| of each other.
   FP64 mode: Nbound, Mbound, iterations, frames and bound energies bit for
-    bit, the order up to runs of equal energy.  Cells below
-    TreeNodeResolution are split by the reference with its process-global
-    drand48 stream (src/oct_tree.tpp:112-123) and kept whole here, so a
-    subhalo holding such a cell may differ in the last bits of a few energies
-    (within 1e-5 * max|E_bound|) and in a few interactions (1e-5 relative);
-    the test counts those subhaloes and requires the rest to be exact.
+    bit, the order up to runs of equal energy, except in subhaloes where the
+    reference split a cell at random: those may differ in the last bits of a
+    few energies (within 1e-5 * max|E_bound|) and in a few interactions (1e-5
+    relative); the test counts them and requires every other subhalo to be
+    exact.
 """
 import numpy as np
 import pytest
@@ -80,12 +86,6 @@ def refined_energies(orc, p, b, a, orf, nbr, r, max_sample):
     return e
 
 
-def straddles(batch, a, b):
-    """True if the subhalo's particles lie on both sides of a periodic face."""
-    x = np.asarray(batch["pos"][a:b], np.float64)
-    return bool(np.any(x.max(axis=0) - x.min(axis=0) > 50.0))
-
-
 def compare(batch, got, ref, exact, orc=None, p=None, counts=None):
     """Per-subhalo comparison; returns (changed side, inexact subhaloes)."""
     max_sample = int(p["max_sample_size"]) if p else 0
@@ -109,6 +109,8 @@ def compare(batch, got, ref, exact, orc=None, p=None, counts=None):
         if g["disrupted"] or n <= 1:
             assert nb == nbr and og[0] == orf[0], tag
             continue
+        split = int(r["random_splits"]) > 0  # the reference split a cell at random
+        erel = BAND if split else EREL
         emax = float(np.max(np.abs(erf[:nbr]))) if nbr else 1.0
         if exact:
             assert nb == nbr, tag
@@ -123,16 +125,17 @@ def compare(batch, got, ref, exact, orc=None, p=None, counts=None):
                         er = refined_energies(orc, p, batch, a, orf, nbr, r, max_sample)
                         assert tie_groups_equal(og[:k], orf[:k], er), tag
                     assert tie_groups_equal(og[k:], orf[k:], eg[k:]), tag
-            else:  # a sub-resolution cell (see the module docstring)
+            else:  # a cell split at random by the reference (see the module docstring)
+                assert split, f"{tag}: not exact, and the reference drew no random octant"
                 inexact += 1
                 assert np.max(np.abs(eg[:nb] - erf[:nb])) <= BAND * emax, tag
                 assert abs(g["interactions"] - r["interactions"]) <= 1e-5 * r["interactions"], tag
             continue
         if g["interactions"] != r["interactions"]:
-            assert abs(g["interactions"] - r["interactions"]) <= 1e-6 * r["interactions"], tag
+            rel = 1e-5 if split else 1e-6
+            assert abs(g["interactions"] - r["interactions"]) <= rel * r["interactions"], tag
             if counts is not None:
-                counts.append((s, n, int(g["interactions"] - r["interactions"]),
-                               straddles(batch, a, b)))
+                counts.append((s, n, int(g["interactions"] - r["interactions"]), split))
         mg = np.zeros(n, bool)
         mr = np.zeros(n, bool)
         mg[og[:nb]] = True
@@ -150,14 +153,14 @@ def compare(batch, got, ref, exact, orc=None, p=None, counts=None):
         if len(diff) == 0 and nb:
             e_ref_pid = np.empty(n, np.float64)
             e_ref_pid[orf[:nbr]] = erf[:nbr]
-            assert np.max(np.abs(eg[:nb] - e_ref_pid[og[:nb]])) <= EREL * emax, tag
+            assert np.max(np.abs(eg[:nb] - e_ref_pid[og[:nb]])) <= erel * emax, tag
             if og[0] != orf[0]:
                 if max_sample and nbr > max_sample:  # ordered by the refined energies
                     er = refined_energies(orc, p, batch, a, orf, nbr, r, max_sample)
                     pos = int(np.nonzero(orf[:len(er)] == og[0])[0][0])
-                    assert er[pos] - er[0] <= EREL * float(np.max(np.abs(er))), tag
+                    assert er[pos] - er[0] <= erel * float(np.max(np.abs(er))), tag
                 else:
-                    assert nbr > 1 and erf[1] - erf[0] <= EREL * emax, \
+                    assert nbr > 1 and erf[1] - erf[0] <= erel * emax, \
                         f"{tag}: most-bound particle"
     return changed, inexact
 
@@ -179,9 +182,9 @@ def test_full_batch_against_oracle(batch, orc, max_sample):
         nbound = sum(int(r["nbound"]) for r in got[2])
         print(f"max_sample {max_sample} precision {'fp64' if precision else 'fp32'}: "
               f"nbound {nbound}, {changed} particles changed side (all inside the band), "
-              f"{inexact} subhaloes with sub-resolution cells not bit-exact, "
+              f"{inexact} subhaloes with cells split at random not bit-exact, "
               f"interaction counts not exact in {len(counts)} subhaloes "
-              f"(subhalo, n, difference, straddles a face): {counts[:10]}")
+              f"(subhalo, n, difference, split at random): {counts[:10]}")
         if precision == 1:
             assert inexact <= 20  # of 2000
         # size-independent properties of the outputs
