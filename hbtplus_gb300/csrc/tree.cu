@@ -205,10 +205,11 @@ struct MomCell {
 // Moments of the chunks.  The double arithmetic of a cell issues per warp
 // instruction whatever the number of active lanes, at 1/64 of the FP32 rate on
 // this GPU, so the cells computed together must fill the lanes: a persistent
-// block takes kBatch chunk roots at a time and aligns their subtrees at the
-// bottom, so that step t computes, in every chunk, the cells t levels above
-// its deepest ones, all of them spread over the block's threads, with one
-// barrier per step (every cell's child cells are deeper, so done before it).
+// block takes one large chunk or kBatch small ones at a time and aligns their
+// subtrees at the bottom, so that step t computes, in every chunk, the cells t
+// levels above its deepest ones, all of them spread over the block's threads,
+// with one barrier per step (every cell's child cells are deeper, so done
+// before it).
 // The internal nodes of the Karras subtree over keys [first, last] rooted at
 // node i are nodes first..last-1 when i == first, first+1..last when i == last;
 // a warp lists the octree cells among them by depth in the chunk's own element
@@ -220,8 +221,9 @@ __global__ void __launch_bounds__(kChunkThreads) k_moments_chunks(Ctx c)
   constexpr unsigned kFull = 0xffffffffu;
   constexpr int kWarps = kChunkThreads / 32;
   __shared__ int s_first, s_steps;
-  __shared__ int s_lo[kBatch], s_maxd[kBatch], s_pre[kDepthBins][kBatch + 1];
+  __shared__ int s_maxd[kBatch], s_pre[kDepthBins][kBatch + 1];
   __shared__ int s_cnt[kBatch][kDepthBins], s_start[kBatch][kDepthBins];
+  __shared__ int s_back[kChunkThreads / 32][kDepthBins];  // fill cursors from the back
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int *glist = reinterpret_cast<int *>(c.X);  // the cell-slot scan is no longer needed
   const int nlarge = c.lvl[0], nsmall = c.lvl[3];
@@ -267,16 +269,29 @@ __global__ void __launch_bounds__(kChunkThreads) k_moments_chunks(Ctx c)
       start[lane] = lo + incl - v;
       cnt[lane] = 0;
       __syncwarp();
+      // each depth's cells of two children first, the others from the back,
+      // so that a warp's lanes mostly add the same number of children
+      int *back = s_back[w];
+      back[lane] = v;
+      __syncwarp();
       for (int k = lane; k < nint; k += 32) {
         const int e = lo + k;
         const int d = c.cdepth[e];
         if (d >= 0) {
           const int r = min(max(d - d0, 0), kDepthBins - 1);
-          glist[start[r] + atomicAdd(&cnt[r], 1)] = e;
+          const int4 *slot = reinterpret_cast<const int4 *>(c.cslot + 8 * e);
+          const int4 a = slot[0], b = slot[1];
+          const int kids = (a.x >= 0) + (a.y >= 0) + (a.z >= 0) + (a.w >= 0) + (b.x >= 0) +
+                           (b.y >= 0) + (b.z >= 0) + (b.w >= 0);
+          if (kids == 2)
+            glist[start[r] + atomicAdd(&cnt[r], 1)] = e;
+          else
+            glist[start[r] + atomicSub(&back[r], 1) - 1] = e;
         }
       }
+      __syncwarp();
+      cnt[lane] = v;
       if (lane == 0) {
-        s_lo[j] = lo;
         s_maxd[j] = maxd;
         atomicMax(&s_steps, maxd + 1);
       }

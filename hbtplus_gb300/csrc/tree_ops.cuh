@@ -384,10 +384,19 @@ __device__ __forceinline__ float4 cell_moment_slots(bool bucket, int idx, int en
     cz = __fma_rn(f2d(a.z), w, cz);
   };
   if (!bucket) {
+    // the occupied octants in ascending order; a warp then issues as many
+    // (double) additions as its lanes' largest number of children, not eight
     const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+    unsigned occ = 0;
 #pragma unroll
-    for (int j = 0; j < 8; j++)
-      if (sl[j] > idx && sl[j] < end) add(sl[j]);
+    for (int j = 0; j < 8; j++) occ |= (sl[j] > idx && sl[j] < end ? 1u : 0u) << j;
+    while (occ) {
+      const int j = __ffs(occ) - 1;
+      occ &= occ - 1;
+      const int4 h = j < 4 ? s0 : s1;
+      const int q = j & 3;
+      add(q == 0 ? h.x : (q == 1 ? h.y : (q == 2 ? h.z : h.w)));
+    }
   } else {
 #pragma unroll 4
     for (int k = idx + 1; k < end; k++) add(k);
