@@ -612,8 +612,15 @@ __global__ void __launch_bounds__(kLB) k_kin_chunks(Ctx c)
     v[0] += f2d(fmul(c.eE[sg.off + p], m));
     double dx[3], dv[3];
     for (int j = 0; j < 3; j++) {
-      dx[j] = f2d(fsub(x[j], sg.ref_pos[j]));
-      if (P.periodic) dx[j] = nearest_d(dx[j], P);
+      // the wrap of a float difference below the box size is exact in float
+      // (Sterbenz), so it gives the double wrap's bits without the FP64 pipe
+      const float d = fsub(x[j], sg.ref_pos[j]);
+      if (!P.periodic)
+        dx[j] = f2d(d);
+      else if (fabsf(d) < P.box)
+        dx[j] = f2d(nearest_f(d, P));
+      else
+        dx[j] = nearest_d(f2d(d), P);
       dx[j] = dmul(dx[j], Pa);
       dv[j] = dadd(f2d(fsub(w[j], sg.ref_vel[j])), dmul(PHz, dx[j]));
       v[1] += dmul(dmul(dv[j], dv[j]), md);
