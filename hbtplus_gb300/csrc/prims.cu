@@ -254,11 +254,17 @@ struct Passes {
   int words[kMaxPasses], shifts[kMaxPasses], n;
 };
 
+// Also clears the first pass's look-back words (nstatus) and tile counter.
 __global__ void __launch_bounds__(kBlock) k_os_hist(const unsigned *hi,
                                                     const unsigned long long *lo, long long n,
-                                                    Passes ps, unsigned *ghist)
+                                                    Passes ps, unsigned *ghist, unsigned *status,
+                                                    long long nstatus, int *counter)
 {
   HBTU_KERNEL_PROLOGUE();
+  for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < nstatus;
+       i += (long long)gridDim.x * kBlock)
+    status[i] = 0u;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *counter = 0;
   __shared__ unsigned h[kMaxPasses][256];
   for (int p = 0; p < ps.n; p++) h[p][threadIdx.x] = 0;
   __syncthreads();
@@ -298,10 +304,14 @@ __global__ void __launch_bounds__(kBlock) k_os_offsets(const unsigned *ghist, in
   }
 }
 
+// status / tile_counter: this pass's look-back words and tile counter (zero
+// when it starts); next_status / next_counter: the next pass's, cleared here
+// (each tile its own words) so that no memset runs between passes.
 __global__ void __launch_bounds__(kBlock) k_os_pass(
     const unsigned *hi_in, const unsigned long long *lo_in, const int *val_in, unsigned *hi_out,
     unsigned long long *lo_out, int *val_out, long long n, int word, int shift,
-    const unsigned *goff, unsigned *status, int *tile_counter, int *err)
+    const unsigned *goff, unsigned *status, int *tile_counter, unsigned *next_status,
+    int *next_counter, int *err)
 {
   HBTU_KERNEL_PROLOGUE();
   __shared__ unsigned wcnt[kBlock / 32][256];
@@ -319,6 +329,8 @@ __global__ void __launch_bounds__(kBlock) k_os_pass(
   __syncthreads();
   const int tile = tile_s;
   const long long t0 = (long long)tile * kTile;
+  next_status[(long long)tile * 256 + tid] = 0u;
+  if (tile == 0 && tid == 0) *next_counter = 0;
   // this tile's records: warp w holds tile positions w*256 .. w*256+255, lane-contiguous
   unsigned dg[kItems], rk[kItems], hv[kItems];
   unsigned long long lv[kItems];
@@ -426,7 +438,7 @@ size_t sort_status_words(long long n)
 {
   long long nb = (n + kTile - 1) / kTile;
   if (nb < 1) nb = 1;
-  return (size_t)nb * 256 + 16;  // + the tile counter
+  return 2 * (size_t)nb * 256 + 16;  // two passes' look-back words + their tile counters
 }
 
 void radix_sort(SortBuffers &b, long long n, const int *words, const int *shifts, int npasses,
@@ -457,19 +469,22 @@ void radix_sort(SortBuffers &b, long long n, const int *words, const int *shifts
     ps.shifts[p] = shifts[p];
   }
   // global digit counts of every pass, their offsets, then one kernel per pass
+  // pass p uses status half p & 1 and clears the other half for pass p + 1;
+  // the histogram kernel clears the first pass's half
+  unsigned *half[2] = {b.os_status, b.os_status + 256 * ntiles};
+  int *counter[2] = {reinterpret_cast<int *>(b.os_status + 512 * ntiles),
+                     reinterpret_cast<int *>(b.os_status + 512 * ntiles) + 1};
   HBTU_CUDA(cudaMemsetAsync(b.os_ghist, 0, sizeof(unsigned) * 256 * kMaxPasses, st));
   const unsigned hblocks = (unsigned)std::min<long long>(ntiles, 152 * 4);
-  launch_k(k_os_hist, hblocks, kBlock, 0, st, b.hi_a, b.lo_a, n, ps, b.os_ghist);
+  launch_k(k_os_hist, hblocks, kBlock, 0, st, b.hi_a, b.lo_a, n, ps, b.os_ghist, half[0],
+           256 * ntiles, counter[0]);
   HBTU_LAUNCHED();
   launch_k(k_os_offsets, 1, kBlock, 0, st, b.os_ghist, npasses, b.os_goff);
   HBTU_LAUNCHED();
   for (int p = 0; p < npasses; p++) {
-    HBTU_CUDA(cudaMemsetAsync(b.os_status, 0, sizeof(unsigned) * 256 * ntiles + 64, st));
-    int *tiles = reinterpret_cast<int *>(b.os_status + 256 * ntiles);
     launch_k(k_os_pass, (unsigned)ntiles, kBlock, 0, st, b.hi_a, b.lo_a, b.val_a, b.hi_b, b.lo_b,
-                                                   b.val_b, n, words[p], shifts[p],
-                                                   b.os_goff + 256 * p, b.os_status, tiles,
-                                                   b.error);
+             b.val_b, n, words[p], shifts[p], b.os_goff + 256 * p, half[p & 1], counter[p & 1],
+             half[(p + 1) & 1], counter[(p + 1) & 1], b.error);
     HBTU_LAUNCHED();
     std::swap(b.hi_a, b.hi_b);
     std::swap(b.lo_a, b.lo_b);

@@ -110,12 +110,22 @@ __global__ void k_cube(Ctx c)
   atomicMax(&c.plan->max_levels, levels);
 }
 
-// Octal key of every tree particle of every active subhalo.
+// Octal key of every tree particle of every active subhalo.  Also clears the
+// element's prefix-depth bits, child-cell counts and octant slots (-1) for the
+// cell stages, and the moment work-list counters.
 __global__ void __launch_bounds__(kTB) k_keys(Ctx c, int ntotal)
 {
   HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kTB + threadIdx.x;
+  if (e == 0)
+    for (int k = 0; k < 4; k++) c.lvl[k] = 0;
   if (e >= ntotal) return;
+  c.mask[e] = 0ull;
+  c.pending[e] = 0;
+  c.pending0[e] = 0;
+  int4 *slot = reinterpret_cast<int4 *>(c.cslot + 8 * (size_t)e);
+  slot[0] = make_int4(-1, -1, -1, -1);
+  slot[1] = make_int4(-1, -1, -1, -1);
   const int s = upper_bound_i(c.tree_base, c.S + 1, e) - 1;
   const SegState &sg = c.seg[s];
   const int epos = sg.off + sg.t0 + (e - c.tree_base[s]);
@@ -154,10 +164,20 @@ __global__ void __launch_bounds__(kTB) k_popc(Ctx c, int ntotal)
   c.pcode[e] = e < ntotal ? __popcll(c.mask[e]) : 0;
 }
 
-__global__ void __launch_bounds__(kTB) k_leaves(Ctx c, int ntotal)
+// sib: the sibling-block layout follows; clear its slot counts (X2) and new
+// slot numbers (newidx, -1) here, two slots per element.
+__global__ void __launch_bounds__(kTB) k_leaves(Ctx c, int ntotal, int sib)
 {
   HBTU_KERNEL_PROLOGUE();
   const int e = blockIdx.x * kTB + threadIdx.x;
+  if (sib && e <= ntotal) {
+    c.X2[2 * (size_t)e] = 0;
+    if (e < ntotal) {
+      c.X2[2 * (size_t)e + 1] = 0;
+      c.newidx[2 * (size_t)e] = -1;
+      c.newidx[2 * (size_t)e + 1] = -1;
+    }
+  }
   if (e >= ntotal) return;
   const int s = c.sb.hi_a[e];
   const int base = c.tree_base[s], n = c.tree_base[s + 1] - base;
@@ -432,11 +452,6 @@ void launch_tree_build(Ctx &c, const PassPlan &pl)
     shifts[np++] = 8 * p;
   }
   radix_sort(c.sb, n, words, shifts, np, c.st);
-  HBTU_CUDA(cudaMemsetAsync(c.mask, 0, sizeof(unsigned long long) * (size_t)n, c.st));
-  HBTU_CUDA(cudaMemsetAsync(c.pending, 0, sizeof(int) * (size_t)n, c.st));
-  HBTU_CUDA(cudaMemsetAsync(c.pending0, 0, sizeof(int) * (size_t)n, c.st));
-  HBTU_CUDA(cudaMemsetAsync(c.lvl, 0, sizeof(int) * 4, c.st));
-  HBTU_CUDA(cudaMemsetAsync(c.cslot, 0xff, sizeof(int) * 8 * (size_t)n, c.st));
   launch_k(k_karras, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
   launch_k(k_cells, nblk(n), kTB, 0, c.st, c, n);
@@ -444,7 +459,8 @@ void launch_tree_build(Ctx &c, const PassPlan &pl)
   launch_k(k_popc, nblk(n + 1), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
   exclusive_scan_i64(c.pcode, c.X, n + 1, c.scan_tmp, c.st);
-  launch_k(k_leaves, nblk(n), kTB, 0, c.st, c, n);
+  const int sib = sibling_walk(c, pl) ? 1 : 0;
+  launch_k(k_leaves, nblk(n + 1), kTB, 0, c.st, c, n, sib);
   HBTU_LAUNCHED();
   launch_k(k_cellnodes, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
@@ -559,9 +575,7 @@ void launch_sibling_layout(Ctx &c, const PassPlan &pl)
 {
   const int n = pl.ntree_total;
   if (n <= 0 || !c.nd2) return;
-  const int nslots = 2 * n;
-  HBTU_CUDA(cudaMemsetAsync(c.X2, 0, sizeof(long long) * (size_t)(nslots + 1), c.st));
-  HBTU_CUDA(cudaMemsetAsync(c.newidx, 0xff, sizeof(int) * (size_t)nslots, c.st));  // -1
+  const int nslots = 2 * n;  // X2 and newidx were cleared by k_leaves
   launch_k(k_sib_count, nblk(n), kTB, 0, c.st, c, n);
   HBTU_LAUNCHED();
   exclusive_scan_i64(c.X2, c.X2, nslots + 1, c.scan_tmp2, c.st);
