@@ -211,9 +211,18 @@ __global__ void __launch_bounds__(kWB) k_walk_fp64(Ctx c, int total)
 // with wp' the derivative of the cubic-spline kernel; dx = x_node - x_target.
 // The walk is walk_lean's (one target per lane, the same nodes in the same
 // order, the potential in the same compensated float sum); the gradient
-// terms go into float partial sums flushed into double every 16 steps, so a
-// target's results do not depend on the other targets of the call.  kGrad =
+// terms go into compensated float sums, one per lane, so a target's results do
+// not depend on the other targets of the call.  kGrad =
 // false computes only the energies (the forward pass of the autograd function).
+// s += v in a compensated float sum (Kahan): s - c carries the sum.
+__device__ __forceinline__ void kahan_add(float &s, float &c, float v)
+{
+  const float y = __fsub_rn(v, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
 template <bool kSib, bool kGrad>
 __device__ __forceinline__ double walk_grad(const WNode *nodes, const Target &t,
                                             const DevParams &P, double (&acc)[3])
@@ -221,8 +230,10 @@ __device__ __forceinline__ double walk_grad(const WNode *nodes, const Target &t,
   const float hf = (float)P.h, hinvf = (float)P.h_inv, h2f = hf * hf;
   const double th2d = (double)P.theta2;
   float hi = 0.f, comp = 0.f;  // Kahan sum of the potential
-  float ax = 0.f, ay = 0.f, az = 0.f;
-  acc[0] = acc[1] = acc[2] = 0.;
+  // compensated (Kahan) float sums of the gradient: no double arithmetic in the
+  // loop, where the lanes of a warp drift apart and a double instruction would
+  // issue once per drifting group of lanes
+  float ax = 0.f, ay = 0.f, az = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
   int iters = 0;
   int cur = t.nxt;
   const int end = t.end;
@@ -262,17 +273,11 @@ __device__ __forceinline__ double walk_grad(const WNode *nodes, const Target &t,
         w = r2 > 0.f ? hinvf * hinvf * dwp * rinv : 0.f;
       }
       const float mw = mass * w;
-      ax += mw * dx;
-      ay += mw * dy;
-      az += mw * dz;
+      kahan_add(ax, cx, mw * dx);
+      kahan_add(ay, cy, mw * dy);
+      kahan_add(az, cz, mw * dz);
     }
     iters++;
-    if (kGrad && (iters & 15) == 0) {
-      acc[0] += (double)ax;
-      acc[1] += (double)ay;
-      acc[2] += (double)az;
-      ax = ay = az = 0.f;
-    }
     if (kSib) {
       cur = open ? nm.w : nm.y;
       if (iters >= steps || cur < t.nxt) break;  // malformed pointers: stop
@@ -280,9 +285,9 @@ __device__ __forceinline__ double walk_grad(const WNode *nodes, const Target &t,
       cur = open ? cur + 1 : max(nm.y, cur + 1);
     }
   }
-  acc[0] += (double)ax;
-  acc[1] += (double)ay;
-  acc[2] += (double)az;
+  acc[0] = dsub((double)ax, (double)cx);
+  acc[1] = dsub((double)ay, (double)cy);
+  acc[2] = dsub((double)az, (double)cz);
   const double base = (double)__fdiv_rn(t.mself, P.eps);  // cancels the self term
   return dadd(dadd(base, (double)hi), -(double)comp);
 }
