@@ -165,74 +165,66 @@ __device__ __forceinline__ unsigned block_excl_scan_u32(unsigned v, unsigned *ws
   return before + x - v;
 }
 
-// Every pass of a sort of at most kSmallN records in one block, the records
-// held in shared memory between passes: the same stable histogram /
-// scan / ranked-scatter steps as the multi-block passes, without a launch
-// per step.
-constexpr int kSmallN = 2 * kTile;  // 4096 records, 128 KB of shared memory
+// Sorts of at most kSmallN records go by rank counting, over many blocks
+// (one launch, instead of a kernel per digit): a record's composite key
+// packs its digits with the last digit most significant (the order the LSD
+// passes produce), and its place is the number of records with a smaller key,
+// or an equal key and a smaller index (so the sort is stable).  Each block
+// holds every record's key in shared memory; kRankSplit threads share one
+// record's count.
+constexpr int kSmallN = 2 * kTile;  // 4096 records
+constexpr int kRankSplit = 8;
 
 struct SmallSortPasses {
   int words[16], shifts[16], n;
 };
 
-__global__ void __launch_bounds__(kBlock) k_rs_small(unsigned *hi_g, unsigned long long *lo_g,
-                                                     int *val_g, int n, SmallSortPasses ps)
+constexpr size_t kRankSmem = (size_t)kSmallN * 2 * sizeof(unsigned long long);
+
+__global__ void __launch_bounds__(kBlock) k_rank_small(const unsigned *hi, const unsigned long long *lo,
+                                                       const int *val, unsigned *hi_o,
+                                                       unsigned long long *lo_o, int *val_o, int n,
+                                                       SmallSortPasses ps)
 {
   HBTU_KERNEL_PROLOGUE();
   extern __shared__ __align__(16) unsigned char smem[];
-  // two buffers of each field: field(b) + b * kSmallN
-  unsigned long long *const lo0 = (unsigned long long *)smem;
-  unsigned *const hi0 = (unsigned *)(lo0 + 2 * kSmallN);
-  int *const val0 = (int *)(hi0 + 2 * kSmallN);
-  __shared__ unsigned wcnt[kBlock / 32][256];
-  __shared__ unsigned toff[256];
-  __shared__ unsigned wsum[kBlock / 32];
-  constexpr int kRounds = kSmallN / kBlock;  // records per lane: warp w owns [w*32*kRounds, ..)
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int e = tid; e < n; e += kBlock) {
-    lo0[e] = lo_g[e];
-    hi0[e] = hi_g[e];
-    val0[e] = val_g[e];
-  }
-  int cur = 0;
-  for (int p = 0; p < ps.n; p++) {
-    const int word = ps.words[p], shift = ps.shifts[p];
-#pragma unroll
-    for (int w = 0; w < kBlock / 32; w++) wcnt[w][tid] = 0;
-    __syncthreads();
-    unsigned dg[kRounds], rk[kRounds];
-#pragma unroll
-    for (int r = 0; r < kRounds; r++) {
-      const int e = warp * 32 * kRounds + r * 32 + lane;
-      dg[r] = e < n ? rs_digit(hi0[cur * kSmallN + e], lo0[cur * kSmallN + e], word, shift)
-                    : 256u + lane;
+  unsigned long long *const kh = (unsigned long long *)smem;  // digits 8..15
+  unsigned long long *const kl = kh + kSmallN;                // digits 0..7
+  for (int e = threadIdx.x; e < n; e += kBlock) {
+    const unsigned h = hi[e];
+    const unsigned long long l = lo[e];
+    unsigned long long a = 0, b = 0;
+    for (int p = 0; p < ps.n; p++) {
+      const unsigned long long d = rs_digit(h, l, ps.words[p], ps.shifts[p]);
+      if (p < 8)
+        a |= d << (8 * p);
+      else
+        b |= d << (8 * (p - 8));
     }
-    warp_rank<kRounds>(dg, rk, wcnt);
-    __syncthreads();
-    const unsigned cnt = warp_offsets(wcnt);
-    toff[tid] = block_excl_scan_u32(cnt, wsum);  // start of digit tid
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < kRounds; r++) {
-      const int e = warp * 32 * kRounds + r * 32 + lane;
-      if (e >= n) continue;
-      const unsigned d = dg[r];
-      const unsigned dst = toff[d] + wcnt[warp][d] + rk[r];
-      hi0[(cur ^ 1) * kSmallN + dst] = hi0[cur * kSmallN + e];
-      lo0[(cur ^ 1) * kSmallN + dst] = lo0[cur * kSmallN + e];
-      val0[(cur ^ 1) * kSmallN + dst] = val0[cur * kSmallN + e];
-    }
-    __syncthreads();
-    cur ^= 1;
+    kl[e] = a;
+    kh[e] = b;
   }
-  for (int e = tid; e < n; e += kBlock) {
-    lo_g[e] = lo0[cur * kSmallN + e];
-    hi_g[e] = hi0[cur * kSmallN + e];
-    val_g[e] = val0[cur * kSmallN + e];
+  __syncthreads();
+  const int rec = blockIdx.x * (kBlock / kRankSplit) + threadIdx.x / kRankSplit;
+  const int part = threadIdx.x % kRankSplit;
+  unsigned cnt = 0;
+  unsigned long long mh = 0, ml = 0;
+  if (rec < n) {
+    mh = kh[rec];
+    ml = kl[rec];
+    for (int j = part; j < n; j += kRankSplit) {
+      const unsigned long long h = kh[j], l = kl[j];
+      cnt += (h < mh) || (h == mh && (l < ml || (l == ml && j < rec)));
+    }
+  }
+#pragma unroll
+  for (int o = kRankSplit / 2; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if (rec < n && part == 0) {
+    hi_o[cnt] = hi[rec];
+    lo_o[cnt] = lo[rec];
+    val_o[cnt] = val[rec];
   }
 }
-
-constexpr size_t kSmallSortSmem = (size_t)kSmallN * 2 * (8 + 4 + 4);
 
 // ---------------------------------------------------------------- onesweep
 // Larger sorts: one kernel per digit (Adinets & Merrill 2022, "Onesweep").
@@ -447,16 +439,21 @@ void radix_sort(SortBuffers &b, long long n, const int *words, const int *shifts
   if (n <= 1 || npasses <= 0) return;
   if (n <= kSmallN && npasses <= 16) {
     // more than 48 KB of shared memory needs an opt-in (per device, so every time)
-    HBTU_CUDA(cudaFuncSetAttribute(k_rs_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)kSmallSortSmem));
+    HBTU_CUDA(cudaFuncSetAttribute(k_rank_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kRankSmem));
     SmallSortPasses ps;
     ps.n = npasses;
     for (int p = 0; p < npasses; p++) {
       ps.words[p] = words[p];
       ps.shifts[p] = shifts[p];
     }
-    launch_k(k_rs_small, 1, kBlock, kSmallSortSmem, st, b.hi_a, b.lo_a, b.val_a, (int)n, ps);
+    const int per_block = kBlock / kRankSplit;
+    launch_k(k_rank_small, (unsigned)((n + per_block - 1) / per_block), kBlock, kRankSmem, st,
+             b.hi_a, b.lo_a, b.val_a, b.hi_b, b.lo_b, b.val_b, (int)n, ps);
     HBTU_LAUNCHED();
+    std::swap(b.hi_a, b.hi_b);  // the result lands in *_a
+    std::swap(b.lo_a, b.lo_b);
+    std::swap(b.val_a, b.val_b);
     return;
   }
   if (npasses > kMaxPasses)
