@@ -20,10 +20,10 @@
 //      pointer that leaves the tree is stored as kDone);
 //   6. bottom-up mass and centre of mass over each cell's children in octant
 //      order, in double, rounded to float per cell as the reference does
-//      (ProcessNode / FillNodeCenter, src/gravity_tree.cpp:18-46): one
-//      thread block per subtree of at most kChunkKeys particles, depth by
-//      depth between block barriers, then an atomic-countdown climb over the
-//      few cells above those subtrees.
+//      (ProcessNode / FillNodeCenter, src/gravity_tree.cpp:18-46): the
+//      subtrees of at most kChunkKeys particles in batches per thread block,
+//      one level per step between block barriers, then an atomic-countdown
+//      climb over the few cells above those subtrees.
 #include <algorithm>
 
 #include "tree_ops.cuh"
@@ -33,8 +33,8 @@ namespace {
 
 constexpr int kTB = 256;
 // Moments: a cell whose subtree holds at most kChunkKeys particles and whose
-// parent's holds more (or that is a root) is a chunk root; a block computes
-// the cells of kBatch chunks at a time.  Cells above the chunk roots are top
+// parent's holds more (or that is a root) is a chunk root, and a block
+// computes the cells of its chunks.  Cells above the chunk roots are top
 // cells.
 constexpr int kChunkKeys = 2048;
 constexpr int kChunkThreads = 256;
