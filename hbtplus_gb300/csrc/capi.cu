@@ -270,11 +270,12 @@ hbtu_status setup_call(hbtu_handle *h, const hbtu_particles *p, long long S, con
                               cudaMemcpyHostToDevice, c.st));
     HBTU_CUDA(cudaMemcpyAsync(c.seg_order, order.data(), sizeof(int) * S, cudaMemcpyHostToDevice,
                               c.st));
-    // the staging copies above read host memory that lives until the call returns
+    // segs, segoff and order are pageable host temporaries: a copy from pageable
+    // memory returns once its source has been staged, so they may go out of
+    // scope now, and the host goes on queueing the call's kernels
   }
   HBTU_CUDA(cudaMemsetAsync(c.plan, 0, sizeof(PassPlan), c.st));
   if (N > 0) launch_init(c, pos, vel, mass, id);
-  HBTU_CUDA(cudaStreamSynchronize(c.st));  // segs/segoff are host temporaries
   return HBTU_OK;
 }
 
