@@ -25,75 +25,65 @@ constexpr int kPlanThreads = 1024;
 inline unsigned nblk(long long n, int b = kLB) { return (unsigned)((n + b - 1) / b); }
 
 // Exclusive scan over segments of up to 4 counters, one block of 1024 threads.
-// The getter is a template argument so it inlines: each thread's segments are
-// then read with independent loads in flight (an indirect call per segment
-// serialises them).
+// Warp w owns a contiguous run of segments (a multiple of 32 long) and its
+// lanes read consecutive segments, so a warp's loads are coalesced and
+// independent: a first sweep sums the run, one warp scans the 32 run totals,
+// a second sweep scans the run 32 segments at a time on top of its start.  The
+// getter is a template argument so it inlines.
 template <int (*getter)(const Ctx &, int, int *)>
 __device__ void plan_scan4(int S, const Ctx &c, int *out0, int *out1, int *out2, int *out3,
                            int *tot)
 {
-  __shared__ int wsum[4][kPlanThreads / 32];
-  const int per = (S + kPlanThreads - 1) / kPlanThreads;
-  const int b = threadIdx.x * per, e = min(S, b + per);
+  constexpr int kWarps = kPlanThreads / 32;
+  static_assert(kWarps == 32, "one lane of warp 0 per warp");
+  constexpr unsigned kFull = 0xffffffffu;
+  __shared__ int wsum[4][kWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int per = ((S + kWarps - 1) / kWarps + 31) & ~31;
+  const int b = w * per, e = min(S, b + per);
   int loc[4] = {0, 0, 0, 0}, v[4];
-  constexpr int kKeep = 4;  // segments per thread whose counters stay in registers
-  int kept[kKeep][4];
-#pragma unroll
-  for (int q = 0; q < kKeep; q++)
-    if (b + q < e) {
-      getter(c, b + q, kept[q]);
-      for (int k = 0; k < 4; k++) loc[k] += kept[q][k];
-    }
-  for (int s = b + kKeep; s < e; s++) {
+  for (int s = b + lane; s < e; s += 32) {
     getter(c, s, v);
     for (int k = 0; k < 4; k++) loc[k] += v[k];
   }
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int inc[4];
   for (int k = 0; k < 4; k++) {
-    int x = loc[k];
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    inc[k] = x;
-    if (lane == 31) wsum[k][w] = x;
+    loc[k] = __reduce_add_sync(kFull, loc[k]);
+    if (lane == 0) wsum[k][w] = loc[k];
   }
   __syncthreads();
   if (w == 0) {
     for (int k = 0; k < 4; k++) {
-      int x = wsum[k][lane];
+      const int t = wsum[k][lane];
+      int x = t;
       for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, x, o);
+        const int y = __shfl_up_sync(kFull, x, o);
         if (lane >= o) x += y;
       }
-      wsum[k][lane] = x;
+      wsum[k][lane] = x - t;  // start of warp lane's run
+      if (lane == 31) tot[k] = x;
     }
   }
   __syncthreads();
-  int run[4];
-  for (int k = 0; k < 4; k++) run[k] = (w > 0 ? wsum[k][w - 1] : 0) + inc[k] - loc[k];
   int *outs[4] = {out0, out1, out2, out3};
-#pragma unroll
-  for (int q = 0; q < kKeep; q++)
-    if (b + q < e)
-      for (int k = 0; k < 4; k++) {
-        if (outs[k]) outs[k][b + q] = run[k];
-        run[k] += kept[q][k];
+  int run[4];
+  for (int k = 0; k < 4; k++) run[k] = wsum[k][w];
+  for (int s0 = b; s0 < e; s0 += 32) {
+    const int s = s0 + lane;
+    int x[4] = {0, 0, 0, 0};
+    if (s < e) getter(c, s, x);
+    for (int k = 0; k < 4; k++) {
+      int inc = x[k];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, inc, o);
+        if (lane >= o) inc += y;
       }
-  for (int s = b + kKeep; s < e; s++) {
-    getter(c, s, v);
-    for (int k = 0; k < 4; k++) {
-      if (outs[k]) outs[k][s] = run[k];
-      run[k] += v[k];
+      if (s < e && outs[k]) outs[k][s] = run[k] + inc - x[k];
+      run[k] += __shfl_sync(kFull, inc, 31);
     }
   }
-  if (threadIdx.x == kPlanThreads - 1) {
-    for (int k = 0; k < 4; k++) {
-      tot[k] = run[k];
-      if (outs[k]) outs[k][S] = run[k];
-    }
-  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 4; k++)
+      if (outs[k]) outs[k][S] = tot[k];
   __syncthreads();
 }
 
