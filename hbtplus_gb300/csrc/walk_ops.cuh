@@ -265,6 +265,23 @@ __device__ __forceinline__ double fp64_contrib(double r2, double mass, const Dev
 // float coordinates (nd_abs), NEAREST per interaction, the reference's
 // arithmetic and summation order.  Returns the potential sum (self term
 // cancelled, before G/a).
+// NEAREST((double)x - (double)q) for float coordinates, as the reference
+// forms a node-target separation.  When the float difference s is exact (a
+// float TwoSum with a zero error term) it is the double difference, and for
+// |s| < box its wrap is exact in float as well (Sterbenz), so the double pipe
+// (1/64 of the FP32 rate on this GPU) only converts the result; otherwise the
+// double path.
+__device__ __forceinline__ double sep_fp64(float x, float q, const DevParams &P)
+{
+  const float s = __fsub_rn(x, q);
+  const float bb = __fsub_rn(s, x);
+  const float err = __fadd_rn(__fsub_rn(x, __fsub_rn(s, bb)), __fsub_rn(-q, bb));
+  if (err == 0.f && !P.periodic) return f2d(s);
+  if (err == 0.f && fabsf(s) < P.box) return f2d(nearest_f(s, P));
+  const double d = dsub(f2d(x), f2d(q));
+  return P.periodic ? nearest_d(d, P) : d;
+}
+
 __device__ __forceinline__ double walk_fp64(const Ctx &c, const Target &t, int *ninter)
 {
   const DevParams &P = c.P;
@@ -276,16 +293,11 @@ __device__ __forceinline__ double walk_fp64(const Ctx &c, const Target &t, int *
   while (cur < end) {
     const float4 na = c.nd_abs[cur];
     const int2 nm = make_int2(c.nd[cur].m.x, c.nd[cur].m.y);
-    double dx = dsub((double)na.x, (double)t.q[0]);
-    double dy = dsub((double)na.y, (double)t.q[1]);
-    double dz = dsub((double)na.z, (double)t.q[2]);
-    if (P.periodic) {
-      dx = nearest_d(dx, P);
-      dy = nearest_d(dy, P);
-      dz = nearest_d(dz, P);
-    }
+    const double dx = sep_fp64(na.x, t.q[0], P);
+    const double dy = sep_fp64(na.y, t.q[1], P);
+    const double dz = sep_fp64(na.z, t.q[2], P);
     const double r2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
-    if ((double)__int_as_float(nm.x & 0x7fffffff) > dmul(r2, th2d)) {
+    if (f2d(__int_as_float(nm.x & 0x7fffffff)) > dmul(r2, th2d)) {
       cur = cur + 1;
     } else {
       const int sk = nm.y;
