@@ -24,15 +24,89 @@ constexpr int kPlanThreads = 1024;
 
 inline unsigned nblk(long long n, int b = kLB) { return (unsigned)((n + b - 1) / b); }
 
-// Exclusive scan over segments of up to 4 counters, one block of 1024 threads.
-// Warp w owns a contiguous run of segments (a multiple of 32 long) and its
+// Exclusive scan over segments of up to 4 counters, one block of 1024 threads,
+// each thread owning a contiguous run of segments (a few, for up to a few
+// thousand subhaloes).  The getter is a template argument so it inlines: each
+// thread's segments are then read with independent loads in flight (an
+// indirect call per segment serialises them).
+template <int (*getter)(const Ctx &, int, int *)>
+__device__ void plan_scan4_thread(int S, const Ctx &c, int *out0, int *out1, int *out2, int *out3,
+                           int *tot)
+{
+  __shared__ int wsum[4][kPlanThreads / 32];
+  const int per = (S + kPlanThreads - 1) / kPlanThreads;
+  const int b = threadIdx.x * per, e = min(S, b + per);
+  int loc[4] = {0, 0, 0, 0}, v[4];
+  constexpr int kKeep = 4;  // segments per thread whose counters stay in registers
+  int kept[kKeep][4];
+#pragma unroll
+  for (int q = 0; q < kKeep; q++)
+    if (b + q < e) {
+      getter(c, b + q, kept[q]);
+      for (int k = 0; k < 4; k++) loc[k] += kept[q][k];
+    }
+  for (int s = b + kKeep; s < e; s++) {
+    getter(c, s, v);
+    for (int k = 0; k < 4; k++) loc[k] += v[k];
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc[4];
+  for (int k = 0; k < 4; k++) {
+    int x = loc[k];
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    inc[k] = x;
+    if (lane == 31) wsum[k][w] = x;
+  }
+  __syncthreads();
+  if (w == 0) {
+    for (int k = 0; k < 4; k++) {
+      int x = wsum[k][lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      wsum[k][lane] = x;
+    }
+  }
+  __syncthreads();
+  int run[4];
+  for (int k = 0; k < 4; k++) run[k] = (w > 0 ? wsum[k][w - 1] : 0) + inc[k] - loc[k];
+  int *outs[4] = {out0, out1, out2, out3};
+#pragma unroll
+  for (int q = 0; q < kKeep; q++)
+    if (b + q < e)
+      for (int k = 0; k < 4; k++) {
+        if (outs[k]) outs[k][b + q] = run[k];
+        run[k] += kept[q][k];
+      }
+  for (int s = b + kKeep; s < e; s++) {
+    getter(c, s, v);
+    for (int k = 0; k < 4; k++) {
+      if (outs[k]) outs[k][s] = run[k];
+      run[k] += v[k];
+    }
+  }
+  if (threadIdx.x == kPlanThreads - 1) {
+    for (int k = 0; k < 4; k++) {
+      tot[k] = run[k];
+      if (outs[k]) outs[k][S] = run[k];
+    }
+  }
+  __syncthreads();
+}
+
+// The same scan for many subhaloes (the gathered plans): warp w owns a
+// contiguous run of segments (a multiple of 32 long) and its
 // lanes read consecutive segments, so a warp's loads are coalesced and
 // independent: a first sweep sums the run, one warp scans the 32 run totals,
 // a second sweep scans the run 32 segments at a time on top of its start.  The
 // getter is a template argument so it inlines.
 template <int (*getter)(const Ctx &, int, int *)>
-__device__ void plan_scan4(int S, const Ctx &c, int *out0, int *out1, int *out2, int *out3,
-                           int *tot)
+__device__ void plan_scan4_warp(int S, const Ctx &c, int *out0, int *out1, int *out2, int *out3,
+                                int *tot)
 {
   constexpr int kWarps = kPlanThreads / 32;
   static_assert(kWarps == 32, "one lane of warp 0 per warp");
@@ -248,9 +322,9 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode, int gath
       c.plan->max_nlast = maxn;
     }
     if (gathered)
-      plan_scan4<get_cnt>(c.S, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
+      plan_scan4_warp<get_cnt>(c.S, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
     else
-      plan_scan4<get_pass>(c.S, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
+      plan_scan4_thread<get_pass>(c.S, c, c.tree_base, c.tchunk_base, nullptr, c.ub_base, tot);
     if (threadIdx.x == 0) {
       c.plan->ntree_total = tot[0];
       c.plan->nchunks_tree = tot[1];
@@ -259,13 +333,13 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode, int gath
     }
     __syncthreads();
     if (gathered) {
-      plan_scan4<get_cnt2>(c.S, c, c.tgt_base, nullptr, nullptr, nullptr, tot);
+      plan_scan4_warp<get_cnt2>(c.S, c, c.tgt_base, nullptr, nullptr, nullptr, tot);
       if (threadIdx.x == 0) {
         c.plan->ntgt_total = tot[0];
         c.plan->nactive = tot[1];
       }
     } else {
-      plan_scan4<get_targets_sorted>(c.S, c, c.tgt_base, nullptr, nullptr, nullptr, tot);
+      plan_scan4_thread<get_targets_sorted>(c.S, c, c.tgt_base, nullptr, nullptr, nullptr, tot);
       if (threadIdx.x == 0) {
         c.plan->ntgt_total = tot[0];
         c.plan->nactive = nact;
@@ -273,15 +347,15 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode, int gath
     }
   } else if (mode == 1) {
     if (gathered)
-      plan_scan4<get_cnt>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
+      plan_scan4_warp<get_cnt>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
     else
-      plan_scan4<get_bound>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
+      plan_scan4_thread<get_bound>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
     if (threadIdx.x == 0) c.plan->nchunks_bound = tot[0];
   } else if (mode == 2) {
     if (gathered)
-      plan_scan4<get_cnt>(c.S, c, c.bchunk_base, c.ub_base, nullptr, nullptr, tot);
+      plan_scan4_warp<get_cnt>(c.S, c, c.bchunk_base, c.ub_base, nullptr, nullptr, tot);
     else
-      plan_scan4<get_final>(c.S, c, c.bchunk_base, c.ub_base, nullptr, nullptr, tot);
+      plan_scan4_thread<get_final>(c.S, c, c.bchunk_base, c.ub_base, nullptr, nullptr, tot);
     if (threadIdx.x == 0) {
       c.plan->nchunks_bound = tot[0];
       c.plan->nsort_total = tot[1];
@@ -289,9 +363,9 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan(Ctx c, int mode, int gath
     }
   } else {
     if (gathered)
-      plan_scan4<get_cnt>(c.S, c, c.ub_base, nullptr, nullptr, nullptr, tot);
+      plan_scan4_warp<get_cnt>(c.S, c, c.ub_base, nullptr, nullptr, nullptr, tot);
     else
-      plan_scan4<get_refine>(c.S, c, c.ub_base, nullptr, nullptr, nullptr, tot);
+      plan_scan4_thread<get_refine>(c.S, c, c.ub_base, nullptr, nullptr, nullptr, tot);
     if (threadIdx.x == 0) c.plan->nsort_total = tot[0];
   }
 }
@@ -778,7 +852,10 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_all(Ctx c)
 {
   HBTU_KERNEL_PROLOGUE();
   __shared__ int tot[4];
-  plan_scan4<get_all_chunks>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
+  if (c.S >= kPlanGatherMin)
+    plan_scan4_warp<get_all_chunks>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
+  else
+    plan_scan4_thread<get_all_chunks>(c.S, c, c.bchunk_base, nullptr, nullptr, nullptr, tot);
 }
 
 }  // namespace
