@@ -111,3 +111,29 @@ def test_oracle_matches_reference_random_inputs(orc):
         assert r1["mbound"] == r2["mbound"]
         if r1["converged"]:
             assert tie_groups_equal(o1, o2, e1)
+
+
+def test_oracle_counts_random_octant_draws(orc):
+    """random_splits counts the drand48 draws of a subhalo's unbinding: none for
+    a cloud with no pair closer than the tree resolution (0.1 softening), some
+    for every seed when particles sit closer than it (src/oct_tree.tpp:112-123;
+    how many depends on where the earlier draws put the particles)."""
+    from hbtplus_gb300 import synthetic as S
+    rng = np.random.Generator(np.random.PCG64(91))
+    p = S.default_params()
+    n = 400
+    sub = dict(pos=(50.0 + rng.uniform(-0.5, 0.5, (n, 3))).astype(np.float32),
+               vel=rng.normal(0.0, 5.0, (n, 3)).astype(np.float32),
+               mass=np.full(n, 1e-3, np.float32), id=np.arange(n, dtype=np.int64),
+               type=np.ones(n, np.int32), ref_pos=np.full(3, 50.0, np.float32),
+               ref_vel=np.zeros(3, np.float32), mostbound_pos=np.full(3, 50.0, np.float32),
+               mostbound_vel=np.zeros(3, np.float32), mostbound_id=0)
+    d = np.linalg.norm(sub["pos"][:, None, :].astype(np.float64) - sub["pos"][None, :, :], axis=2)
+    assert np.min(d + np.eye(n)) > 1e-3
+    _, _, res = orc.unbind(p, sub, nthreads=1)
+    assert res["random_splits"] == 0
+    close = dict(sub)
+    close["pos"] = sub["pos"].copy()
+    close["pos"][1:6] = close["pos"][0] + np.float32(1e-5) * np.arange(1, 6, dtype=np.float32)[:, None]
+    for seed in (1, 2, 3):
+        assert orc.unbind(p, close, nthreads=1, drand_seed=seed)[2]["random_splits"] > 0
