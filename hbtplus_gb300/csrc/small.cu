@@ -225,9 +225,9 @@ __device__ void build_tree(const Ctx &c, SegState &sg, int P0, unsigned long lon
     }
   }
   __syncthreads();
-  // moments one octal depth at a time, deepest first (k_moments_level), over
-  // dense per-depth lists of the cells so that every lane of a warp works on a
-  // cell (a warp's double instruction costs the same however few lanes run it)
+  // moments one octal depth at a time, deepest first, over dense per-depth
+  // lists of the cells so that every lane of a warp works on a cell (a warp's
+  // double instruction costs the same however few lanes run it)
   __shared__ int dcount[kMaxLevels + 2], dstart[kMaxLevels + 2];
   if (threadIdx.x < kMaxLevels + 2) dcount[threadIdx.x] = 0;
   __syncthreads();
